@@ -1,0 +1,24 @@
+"""bandedgpu: BandedMatrices.jl's banded hot path (gbmv, banded*banded, banded LU and
+QR, plus batched, mixed-precision and adjoint solves) on one GB300 GPU.
+
+The numerical work runs in libbandedgpu.so (hand-written CUDA for sm_103a behind
+the C ABI in include/bandedgpu.h).  This package is the host-side mirror of the
+reference's Julia interface: a device-resident ``BandedMatrix`` that keeps the
+(l+u+1) x n LAPACK band storage, ``brand``/``brandn``, ``mul_`` (``mul!``),
+``@`` (``*``), ``lu``, ``ldiv_`` (``ldiv!``), ``solve`` (``\\``) and ``qr``.
+"""
+from . import _lib
+from ._lib import BandedGPUError
+from .banded import (BandedMatrix, BandError, DimensionMismatch, band_storage, bandeddata, bandwidth, bandwidths,
+                     brand, brandn, gbmv)
+from .linalg import ldiv, mul, mul_, mul_t_
+
+__all__ = [
+    "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
+    "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
+]
+
+
+def load_library():
+    """Load libbandedgpu.so (raises if it has not been built)."""
+    return _lib.load()

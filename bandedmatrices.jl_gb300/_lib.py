@@ -1,0 +1,74 @@
+"""ctypes binding of libbandedgpu.so (the C ABI declared in include/bandedgpu.h).
+
+This is the Python counterpart of the ``ccall`` bindings a Julia package would
+make.  There is no fallback: if the shared library is missing or no CUDA device
+is present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libbandedgpu.so")
+
+BM_OK = 0
+BM_ERR_CUDA = -1001
+BM_ERR_UNSUPPORTED = -1002
+BM_ERR_NOMEM = -1003
+BM_ERR_ALIGN = -1004
+
+i64 = ctypes.c_int64
+P = ctypes.c_void_p
+D = ctypes.c_double
+F = ctypes.c_float
+C = ctypes.c_char
+I = ctypes.c_int
+
+# name -> argtypes (every entry point returns int)
+SIGNATURES: dict[str, list] = {
+    "bm_version": [],
+    "bm_last_error": [],
+    "bm_device_status": [P, I, P],
+    "bm_dgbmv": [C, i64, i64, i64, i64, D, P, i64, P, i64, D, P, i64, P],
+    "bm_sgbmv": [C, i64, i64, i64, i64, F, P, i64, P, i64, F, P, i64, P],
+}
+
+
+class BandedGPUError(RuntimeError):
+    """A libbandedgpu call failed (illegal argument or CUDA error)."""
+
+
+_lib = None
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Load the shared library (once) and declare every signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise BandedGPUError(
+            f"{path} is missing: build it with __graft_entry__.build() (there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    for name, argt in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = argt
+        fn.restype = ctypes.c_char_p if name == "bm_last_error" else ctypes.c_int
+    _lib = L
+    return L
+
+
+def check(ret: int, name: str) -> None:
+    if ret == BM_OK:
+        return
+    L = load()
+    msg = L.bm_last_error().decode(errors="replace")
+    if ret < 0 and ret > -100:
+        raise BandedGPUError(f"{name}: illegal value of argument {-ret}")
+    raise BandedGPUError(f"{name}: error {ret}: {msg}")
+
+
+def call(name: str, *args) -> None:
+    check(getattr(load(), name)(*args), name)

@@ -1,0 +1,103 @@
+// Shared device/host helpers for the banded kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "../../include/bandedgpu.h"
+
+namespace bm {
+
+typedef int64_t i64;
+
+// ---------------------------------------------------------------- host side
+// Thread-local last-error text (bm_last_error()).
+void set_error(const char* fmt, ...);
+
+// Number of SMs of the current device (cached per device).
+int num_sms();
+
+// Opt a kernel into `bytes` of dynamic shared memory once per device.
+cudaError_t ensure_smem(const void* kernel, int bytes);
+
+// Address of this library's device status word on the current device.
+int* status_word();
+
+inline int cuda_status(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return BM_OK;
+  set_error("%s: %s", where, cudaGetErrorString(e));
+  return BM_ERR_CUDA;
+}
+
+inline int launch_status(const char* where) { return cuda_status(cudaGetLastError(), where); }
+
+inline i64 ceil_div(i64 a, i64 b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------- device side
+// Spin limits.  Every wait in these kernels is bounded: on expiry the kernel
+// records BM_STATUS_TIMEOUT in the status word and stops waiting.
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+enum : int { BM_STATUS_TIMEOUT = 1 };
+
+__device__ __forceinline__ void record_status(int* status, int code) {
+  if (status) atomicOr(status, code);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Order this thread's generic-proxy shared-memory accesses before later
+// async-proxy (bulk copy) writes to the same buffer.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared (TMA engine); src, dst 16-byte aligned and
+// bytes a multiple of 16.  Completion is signalled on `bar` as tx bytes.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `phase` of `bar`.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+  for (uint32_t it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) {
+  return __ldg(p);
+}
+
+}  // namespace bm

@@ -1,0 +1,306 @@
+// gbmv: y <- alpha*op(A)*x + beta*y on LAPACK band storage.
+//
+// Replaces the xGBMV ccall of BandedMatrices.jl (src/blas.jl:16-28; stdlib
+// BLAS.gbmv! from banded_gbmv!, src/generic/matmul.jl:21-23).
+//
+// Fast path (incx = incy = 1, 16-byte aligned A and x): a persistent kernel,
+// one CTA per SM.  Work is cut into tiles of consecutive outputs; for each tile
+// thread 0 streams the band columns the tile touches, and the x window, from
+// HBM into a shared-memory ring of `stages` buffers with 1-D TMA bulk copies
+// (cp.async.bulk, completion on an mbarrier), while all threads reduce the
+// previous buffer.  Each output element is owned by one thread and accumulated
+// in the reference-BLAS order (see below), so the result is deterministic and
+// equal, bit for bit, to reference dgbmv compiled with fused multiply-adds.
+//
+//   'N': y_i = beta*y_i, then y_i = fma(alpha*x_j, A(i,j), y_i) for j ascending
+//        (the column-oriented loop of reference DGBMV);
+//   'T': t = sum_i A(i,j)*x_i accumulated with fma for i ascending,
+//        y_j = fma(alpha, t, beta*y_j).
+//
+// Roofline: HBM.  Algorithmic bytes per call = s*(lda*n + |x| + |y|*(beta!=0 ? 2 : 1)).
+#include "common.cuh"
+
+namespace bm {
+
+template <typename T>
+struct GbmvParams {
+  i64 m, n, kl, ku, lda;
+  T alpha, beta;
+  const T* A;
+  const T* x;
+  T* y;
+  i64 tile;    // outputs per tile
+  i64 ntiles;
+  int stages;
+  uint32_t stage_bytes;  // bytes per ring slot (A part + x part), multiple of 128
+  uint32_t xoff;         // byte offset of the x part inside a slot
+  int* status;
+};
+
+template <typename T>
+struct Region {
+  i64 gs;      // first element held in smem (rounded down to 16 bytes)
+  i64 ge;      // end of the bulk-copied part (rounded down to 16 bytes)
+  i64 end;     // one past the last element needed
+};
+
+template <typename T>
+__device__ __forceinline__ Region<T> make_region(i64 start, i64 end) {
+  constexpr i64 q = 16 / sizeof(T);
+  Region<T> r;
+  if (end <= start) {
+    r.gs = r.ge = r.end = start & ~(q - 1);
+    return r;
+  }
+  r.gs = start & ~(q - 1);
+  r.ge = end & ~(q - 1);
+  if (r.ge < r.gs) r.ge = r.gs;
+  r.end = end;
+  return r;
+}
+
+// Column range of A and element range of x touched by tile t.
+template <typename T, bool TRANS>
+__device__ __forceinline__ void tile_ranges(const GbmvParams<T>& p, i64 t, i64& o0, i64& o1, i64& c0,
+                                            i64& c1, i64& x0, i64& x1) {
+  o0 = t * p.tile;
+  o1 = min(o0 + p.tile, TRANS ? p.n : p.m);
+  if (!TRANS) {
+    c0 = max((i64)0, o0 - p.kl);
+    c1 = min(p.n, o1 + p.ku);
+    if (c1 < c0) c1 = c0;
+    x0 = c0;
+    x1 = c1;
+  } else {
+    c0 = o0;
+    c1 = o1;
+    x0 = max((i64)0, o0 - p.ku);
+    x1 = min(p.m, o1 + p.kl);
+    if (x1 < x0) x1 = x0;
+  }
+}
+
+template <typename T, bool TRANS>
+__device__ __forceinline__ void issue_tile(const GbmvParams<T>& p, unsigned char* slots, uint64_t* bars, i64 k) {
+  const i64 t = (i64)blockIdx.x + k * (i64)gridDim.x;
+  if (t >= p.ntiles) return;
+  const int s = (int)(k % p.stages);
+  i64 o0, o1, c0, c1, x0, x1;
+  tile_ranges<T, TRANS>(p, t, o0, o1, c0, c1, x0, x1);
+  Region<T> ra = make_region<T>(c0 * p.lda, c1 * p.lda);
+  Region<T> rx = make_region<T>(x0, x1);
+  const uint32_t ba = (uint32_t)((ra.ge - ra.gs) * (i64)sizeof(T));
+  const uint32_t bx = (uint32_t)((rx.ge - rx.gs) * (i64)sizeof(T));
+  unsigned char* slot = slots + (size_t)s * p.stage_bytes;
+  fence_proxy_async_smem();
+  mbar_arrive_expect_tx(&bars[s], ba + bx);
+  if (ba) bulk_g2s(slot, p.A + ra.gs, ba, &bars[s]);
+  if (bx) bulk_g2s(slot + p.xoff, p.x + rx.gs, bx, &bars[s]);
+}
+
+template <typename T, bool TRANS>
+__global__ void __launch_bounds__(256) gbmv_tma_kernel(const GbmvParams<T> p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
+  unsigned char* slots = smem + 128;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < p.stages; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < p.stages; ++k) issue_tile<T, TRANS>(p, slots, bars, k);
+
+  i64 k = 0;
+  bool failed = false;
+  for (;; ++k) {
+    const i64 t = (i64)blockIdx.x + k * (i64)gridDim.x;
+    if (t >= p.ntiles) break;
+    const int s = (int)(k % p.stages);
+    const uint32_t phase = (uint32_t)((k / p.stages) & 1);
+    const bool ok = mbar_wait(&bars[s], phase);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    i64 o0, o1, c0, c1, x0, x1;
+    tile_ranges<T, TRANS>(p, t, o0, o1, c0, c1, x0, x1);
+    const Region<T> ra = make_region<T>(c0 * p.lda, c1 * p.lda);
+    const Region<T> rx = make_region<T>(x0, x1);
+    T* sa = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes);
+    T* sx = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes + p.xoff);
+    // Ragged tails (< 16 bytes) that the bulk copies left out.
+    {
+      const int na = (int)(ra.end - ra.ge), nx = (int)(rx.end - rx.ge);
+      const int tid = threadIdx.x;
+      if (tid < na) sa[ra.ge - ra.gs + tid] = p.A[ra.ge + tid];
+      else if (tid >= 32 && tid - 32 < nx) sx[rx.ge - rx.gs + tid - 32] = p.x[rx.ge + tid - 32];
+    }
+    if (!TRANS && p.alpha != T(1)) {
+      __syncthreads();
+      for (i64 e = x0 + threadIdx.x; e < x1; e += blockDim.x) sx[e - rx.gs] = p.alpha * sx[e - rx.gs];
+    }
+    __syncthreads();
+
+    if (!TRANS) {
+      for (i64 i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
+        const i64 jlo = max((i64)0, i - p.kl), jhi = min(p.n - 1, i + p.ku);
+        T acc = (p.beta == T(0)) ? T(0) : p.beta * p.y[i];
+        int ia = (int)(jlo * p.lda + p.ku + i - jlo - ra.gs);
+        int ix = (int)(jlo - rx.gs);
+        const int step = (int)p.lda - 1;
+        for (i64 j = jlo; j <= jhi; ++j) {
+          acc = fma(sx[ix], sa[ia], acc);
+          ia += step;
+          ++ix;
+        }
+        p.y[i] = acc;
+      }
+    } else {
+      for (i64 j = o0 + threadIdx.x; j < o1; j += blockDim.x) {
+        const i64 ilo = max((i64)0, j - p.ku), ihi = min(p.m - 1, j + p.kl);
+        T acc = T(0);
+        int ia = (int)(j * p.lda + p.ku + ilo - j - ra.gs);
+        int ix = (int)(ilo - rx.gs);
+        for (i64 i = ilo; i <= ihi; ++i) {
+          acc = fma(sa[ia], sx[ix], acc);
+          ++ia;
+          ++ix;
+        }
+        const T y0 = (p.beta == T(0)) ? T(0) : p.beta * p.y[j];
+        p.y[j] = fma(p.alpha, acc, y0);
+      }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) issue_tile<T, TRANS>(p, slots, bars, k + p.stages);
+  }
+
+  if (failed) {
+    if (threadIdx.x == 0) record_status(p.status, BM_STATUS_TIMEOUT);
+    // Let copies that are still in flight land before the CTA exits.
+    for (i64 kk = k; kk < k + p.stages; ++kk) {
+      const i64 t = (i64)blockIdx.x + kk * (i64)gridDim.x;
+      if (t >= p.ntiles) break;
+      (void)mbar_wait(&bars[kk % p.stages], (uint32_t)((kk / p.stages) & 1));
+    }
+  }
+}
+
+// Any strides: one thread per output element, same accumulation order.
+template <typename T, bool TRANS>
+__global__ void gbmv_strided_kernel(i64 m, i64 n, i64 kl, i64 ku, T alpha, const T* __restrict__ A, i64 lda,
+                                    const T* __restrict__ x, i64 incx, T beta, T* __restrict__ y, i64 incy) {
+  const i64 leny = TRANS ? n : m, lenx = TRANS ? m : n;
+  const i64 kx = incx > 0 ? 0 : -(lenx - 1) * incx;
+  const i64 ky = incy > 0 ? 0 : -(leny - 1) * incy;
+  for (i64 o = (i64)blockIdx.x * blockDim.x + threadIdx.x; o < leny; o += (i64)gridDim.x * blockDim.x) {
+    T* yp = y + ky + o * incy;
+    if (!TRANS) {
+      const i64 i = o;
+      const i64 jlo = max((i64)0, i - kl), jhi = min(n - 1, i + ku);
+      T acc = (beta == T(0)) ? T(0) : beta * *yp;
+      if (alpha != T(0))
+        for (i64 j = jlo; j <= jhi; ++j) acc = fma(alpha * x[kx + j * incx], A[j * lda + ku + i - j], acc);
+      *yp = acc;
+    } else {
+      const i64 j = o;
+      const i64 ilo = max((i64)0, j - ku), ihi = min(m - 1, j + kl);
+      T acc = T(0);
+      for (i64 i = ilo; i <= ihi; ++i) acc = fma(A[j * lda + ku + i - j], x[kx + i * incx], acc);
+      const T y0 = (beta == T(0)) ? T(0) : beta * *yp;
+      *yp = (alpha == T(0)) ? y0 : fma(alpha, acc, y0);
+    }
+  }
+}
+
+template <typename T>
+static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T* A, i64 lda, const T* x, i64 incx,
+                     T beta, T* y, i64 incy, cudaStream_t stream, const char* name) {
+  const bool notr = (trans == 'N' || trans == 'n');
+  if (!notr && !(trans == 'T' || trans == 't' || trans == 'C' || trans == 'c')) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (kl < 0) return -4;
+  if (ku < 0) return -5;
+  if (lda < kl + ku + 1) return -8;
+  if (incx == 0) return -10;
+  if (incy == 0) return -13;
+  if (m == 0 || n == 0 || (alpha == T(0) && beta == T(1))) return BM_OK;
+  const i64 leny = notr ? m : n;
+  const int nsm = num_sms();
+
+  const bool aligned = ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(x)) & 15) == 0;
+  if (incx != 1 || incy != 1 || !aligned || alpha == T(0) || (lda * n) >= ((i64)1 << 40)) {
+    const int threads = 256;
+    const i64 blocks = std::min<i64>(ceil_div(leny, threads), (i64)nsm * 32);
+    if (notr)
+      gbmv_strided_kernel<T, false><<<(unsigned)blocks, threads, 0, stream>>>(m, n, kl, ku, alpha, A, lda, x, incx,
+                                                                              beta, y, incy);
+    else
+      gbmv_strided_kernel<T, true><<<(unsigned)blocks, threads, 0, stream>>>(m, n, kl, ku, alpha, A, lda, x, incx,
+                                                                             beta, y, incy);
+    return launch_status(name);
+  }
+
+  // Tile selection: a ring of `stages` slots inside ~200 KB of shared memory.
+  const i64 s = sizeof(T);
+  const i64 budget = 200 * 1024;
+  const i64 halo = kl + ku;
+  const i64 per_out = (lda + 1) * s;  // bytes of A plus x per column
+  int stages = 4;
+  i64 tile = 0;
+  for (int st = 4; st >= 2; --st) {
+    const i64 slot = budget / st;
+    const i64 cols = (slot - 256) / per_out;
+    const i64 tl = notr ? cols - halo : cols - (halo * s + per_out - 1) / per_out;
+    stages = st;
+    tile = tl;
+    if (tl >= 4 * halo && tl >= 256) break;
+  }
+  if (tile < 32) return BM_ERR_UNSUPPORTED;  // band too wide for one slot; not reached for lda <= 2000
+  tile = std::min<i64>(tile, 4096);
+  // Keep at least ~2 tiles per CTA when the problem is small.
+  const i64 want = ceil_div(leny, (i64)nsm * 2);
+  if (want < tile) tile = std::max<i64>(32, ((want + 31) / 32) * 32);
+  GbmvParams<T> p;
+  p.m = m; p.n = n; p.kl = kl; p.ku = ku; p.lda = lda;
+  p.alpha = alpha; p.beta = beta; p.A = A; p.x = x; p.y = y;
+  p.tile = tile;
+  p.ntiles = ceil_div(leny, tile);
+  p.stages = stages;
+  const i64 cols = notr ? tile + halo : tile;
+  const i64 xlen = notr ? tile + halo : tile + halo;
+  const i64 abytes = ((cols * lda + 2 * (16 / s)) * s + 127) / 128 * 128;
+  const i64 xbytes = ((xlen + 2 * (16 / s)) * s + 127) / 128 * 128;
+  p.xoff = (uint32_t)abytes;
+  p.stage_bytes = (uint32_t)(abytes + xbytes);
+  p.status = status_word();
+  const int smem = 128 + stages * (int)p.stage_bytes;
+  const void* kfn = notr ? (const void*)gbmv_tma_kernel<T, false> : (const void*)gbmv_tma_kernel<T, true>;
+  int r = cuda_status(ensure_smem(kfn, smem), name);
+  if (r) return r;
+  const i64 grid = std::min<i64>(p.ntiles, nsm);
+  if (notr)
+    gbmv_tma_kernel<T, false><<<(unsigned)grid, 256, smem, stream>>>(p);
+  else
+    gbmv_tma_kernel<T, true><<<(unsigned)grid, 256, smem, stream>>>(p);
+  return launch_status(name);
+}
+
+}  // namespace bm
+
+extern "C" int bm_dgbmv(char trans, int64_t m, int64_t n, int64_t kl, int64_t ku, double alpha, const double* A,
+                        int64_t lda, const double* x, int64_t incx, double beta, double* y, int64_t incy,
+                        bm_stream_t stream) {
+  return bm::gbmv_impl<double>(trans, m, n, kl, ku, alpha, A, lda, x, incx, beta, y, incy,
+                               reinterpret_cast<cudaStream_t>(stream), "bm_dgbmv");
+}
+
+extern "C" int bm_sgbmv(char trans, int64_t m, int64_t n, int64_t kl, int64_t ku, float alpha, const float* A,
+                        int64_t lda, const float* x, int64_t incx, float beta, float* y, int64_t incy,
+                        bm_stream_t stream) {
+  return bm::gbmv_impl<float>(trans, m, n, kl, ku, alpha, A, lda, x, incx, beta, y, incy,
+                              reinterpret_cast<cudaStream_t>(stream), "bm_sgbmv");
+}

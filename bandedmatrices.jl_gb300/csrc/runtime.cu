@@ -1,0 +1,88 @@
+// Host runtime of the library: error text, device properties, status word.
+#include <cstdarg>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "common.cuh"
+
+namespace bm {
+
+static thread_local char g_err[512] = {0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+static std::mutex g_mu;
+
+int num_sms() {
+  static std::map<int, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int v = 0;
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  if (v <= 0) v = 1;
+  cache[dev] = v;
+  return v;
+}
+
+cudaError_t ensure_smem(const void* kernel, int bytes) {
+  static std::map<std::pair<const void*, int>, int> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_pair(kernel, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done[key] = bytes;
+  return e;
+}
+
+// One status word per device, in this module's static device memory.
+static __device__ int g_status_word;
+
+int* status_word() {
+  static std::map<int, int*> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int* p = nullptr;
+  if (cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_status_word) != cudaSuccess) p = nullptr;
+  cache[dev] = p;
+  return p;
+}
+
+}  // namespace bm
+
+extern "C" int bm_version(void) { return 100; }
+
+extern "C" const char* bm_last_error(void) { return bm::g_err; }
+
+extern "C" int bm_device_status(int* status_out, int clear, bm_stream_t stream) {
+  if (!status_out) return -1;
+  int* w = bm::status_word();
+  if (!w) {
+    bm::set_error("bm_device_status: status word unavailable");
+    return BM_ERR_CUDA;
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int r = bm::cuda_status(cudaMemcpyAsync(status_out, w, sizeof(int), cudaMemcpyDeviceToHost, s),
+                          "bm_device_status");
+  if (r) return r;
+  if (clear) {
+    r = bm::cuda_status(cudaMemsetAsync(w, 0, sizeof(int), s), "bm_device_status");
+    if (r) return r;
+  }
+  return bm::cuda_status(cudaStreamSynchronize(s), "bm_device_status");
+}

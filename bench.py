@@ -1,0 +1,418 @@
+#!/usr/bin/env python3
+"""Benchmark of the banded hot path on one GB300 (or N replicas under torchrun).
+
+Workload (one "step"): the bandwidth-bound sweep -- y = A*x (gbmv) for a square
+n = 2^24 band with l = u in {1, 8, 32}, in Float32 and Float64 band storage,
+entries uniform(-1,1), x randn; plus banded_mul of two n = 2^20, l = u = 16
+matrices (result bandwidth (32,32)) in both precisions.  Every operand set is
+larger than the 129 MB L2, so timed iterations stream from HBM.
+
+value  = algorithmic bytes of all kernels of a step / device time of a step (GB/s)
+e2e    = the same bytes / time of the same step through the public API with
+         host buffers (pinned host -> device copies of A, B and x, and device
+         -> host copies of y and C, inside the timed region)
+--impl reference times the reference's CPU path (OpenBLAS dgbmv/sgbmv, the
+routine BandedMatrices.jl ccalls for A*x, and the _gbmm! column loop over it)
+on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import glob
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "banded LU+solve systems/s & gbmv GB/s vs plain FP64 GPU at 1e-10 backward err"
+GBMV_CASES = [("f32", 1), ("f32", 8), ("f32", 32), ("f64", 1), ("f64", 8), ("f64", 32)]
+N_GBMV = 1 << 24
+N_GBMM, LU_GBMM = 1 << 20, 16
+WORKLOAD = ("gbmv y=A*x, n=2^24 square, l=u in {1,8,32}, f32+f64, uniform(-1,1) band, randn x; "
+            "banded_mul n=2^20 l=u=16 -> (32,32), f32+f64")
+
+
+def gbmv_bytes(n, l, u, s):
+    # band (l+u+1)*n + x n + y n (beta = 0: y written only)
+    return s * n * (l + u + 1 + 2)
+
+
+def gbmm_bytes(n, l, u, s):
+    # A and B (l+u+1)*n each, C (2l+2u+1)*n written
+    return s * n * ((l + u + 1) * 2 + (2 * l + 2 * u + 1))
+
+
+# --------------------------------------------------------------------------- CPU (OpenBLAS)
+def _openblas():
+    import scipy
+
+    libdir = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
+    L = ctypes.CDLL(glob.glob(os.path.join(libdir, "libscipy_openblas*.so"))[0])
+    i, d, f, p = ctypes.c_int, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
+    L.scipy_cblas_dgbmv.argtypes = [i, i, i, i, i, i, d, p, i, p, i, d, p, i]
+    L.scipy_cblas_sgbmv.argtypes = [i, i, i, i, i, i, f, p, i, p, i, f, p, i]
+    L.scipy_cblas_dgbmv.restype = L.scipy_cblas_sgbmv.restype = None
+    L.scipy_openblas_get_num_threads.restype = ctypes.c_int
+    return L
+
+
+def cpu_sweep(steps: int, warmup: int, n_cpu: int = 1 << 21):
+    """Time OpenBLAS gbmv (all host threads) and the _gbmm! column loop on a bounded sample:
+    the same bandwidths and dtypes at n = 2^21 (gbmv) and the full n = 2^20 (gbmm)."""
+    import numpy as np
+
+    L = _openblas()
+    threads = int(L.scipy_openblas_get_num_threads())
+    rng = np.random.default_rng(0)
+    cases = []
+    for dt, lu in GBMV_CASES:
+        nt = np.float32 if dt == "f32" else np.float64
+        A = np.asfortranarray(rng.uniform(-1, 1, (2 * lu + 1, n_cpu)).astype(nt))
+        x = rng.standard_normal(n_cpu).astype(nt)
+        y = np.zeros(n_cpu, dtype=nt)
+        fn = L.scipy_cblas_sgbmv if dt == "f32" else L.scipy_cblas_dgbmv
+        args = (102, 111, n_cpu, n_cpu, lu, lu, 1.0, A.ctypes.data, 2 * lu + 1, x.ctypes.data, 1, 0.0, y.ctypes.data, 1)
+        cases.append((fn, args, gbmv_bytes(n_cpu, lu, lu, nt().itemsize), (A, x, y)))  # keep buffers alive
+    # _gbmm!: one gbmv per column of C (gbmm.jl:296-340), at the full n = 2^20
+    n_mm = 1 << 20
+    mm = []
+    for dt in ("f32", "f64"):
+        nt = np.float32 if dt == "f32" else np.float64
+        A = np.asfortranarray(rng.uniform(-1, 1, (33, n_mm)).astype(nt))
+        B = np.asfortranarray(rng.uniform(-1, 1, (33, n_mm)).astype(nt))
+        C = np.zeros((65, n_mm), dtype=nt, order="F")
+        mm.append((dt, A, B, C, nt().itemsize))
+
+    import oracle  # CPU-baseline leg: the _gbmm! column loop restated in C over OpenBLAS gbmv
+
+    orl = oracle.lib()
+    fptr = {"f32": ctypes.cast(L.scipy_cblas_sgbmv, ctypes.c_void_p).value,
+            "f64": ctypes.cast(L.scipy_cblas_dgbmv, ctypes.c_void_p).value}
+
+    def gbmm_cpu(dt, A, B, C, s):
+        fn = orl.or_sgbmm_percol_cblas if dt == "f32" else orl.or_dgbmm_percol_cblas
+        T = ctypes.c_float if dt == "f32" else ctypes.c_double
+        fn(ctypes.c_void_p(fptr[dt]), n_mm, n_mm, n_mm, LU_GBMM, LU_GBMM, LU_GBMM, LU_GBMM, T(1.0),
+           ctypes.c_void_p(A.ctypes.data), 33, ctypes.c_void_p(B.ctypes.data), 33, T(0.0),
+           ctypes.c_void_p(C.ctypes.data), 65)
+
+    def one_step():
+        t_gbmv = 0.0
+        bytes_gbmv = 0
+        for fn, args, nb, _keep in cases:
+            t0 = time.perf_counter()
+            fn(*args)
+            t_gbmv += time.perf_counter() - t0
+            bytes_gbmv += nb
+        t_mm = 0.0
+        bytes_mm = 0
+        for dt, A, B, C, s in mm:
+            t0 = time.perf_counter()
+            gbmm_cpu(dt, A, B, C, s)
+            t_mm += time.perf_counter() - t0
+            bytes_mm += gbmm_bytes(n_mm, LU_GBMM, LU_GBMM, s)
+        return t_gbmv, bytes_gbmv, t_mm, bytes_mm
+
+    for _ in range(warmup):
+        one_step()
+    samples = [one_step() for _ in range(max(1, steps))]
+    t = sum(s[0] + s[2] for s in samples)
+    by = sum(s[1] + s[3] for s in samples)
+    return {
+        "value": by / t / 1e9,
+        "gbmv_GBps": sum(s[1] for s in samples) / sum(s[0] for s in samples) / 1e9,
+        "gbmm_GBps": sum(s[3] for s in samples) / sum(s[2] for s in samples) / 1e9,
+        "sec_per_step": t / len(samples),
+        "threads": threads,
+        "sample": (f"OpenBLAS {{s,d}}gbmv via SciPy's bundled libscipy_openblas (the BLAS routine "
+                   f"BandedMatrices.jl ccalls; Julia absent), {threads} threads, same l,u,dtypes at n=2^21; "
+                   f"_gbmm! column loop (restated in C) over the same OpenBLAS gbmv at n=2^20"),
+    }
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- GPU
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic(name):
+    """DRAM bytes per launch of a kernel from a committed ncu summary (profiles/*.md)."""
+    for f in glob.glob(os.path.join(ROOT, "profiles", "*.md")):
+        for line in open(f):
+            if line.startswith(f"traffic[{name}]"):
+                try:
+                    return float(line.split("=")[1].split()[0])
+                except (IndexError, ValueError):
+                    pass
+    return None
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import __graft_entry__ as ge
+
+    bm = ge.package()
+    bm.load_library()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1000 + rank)
+
+    gb = []  # (label, A, x, y, bytes)
+    for dt_name, lu in GBMV_CASES:
+        dt = torch.float32 if dt_name == "f32" else torch.float64
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, N_GBMV, dt, dev), N_GBMV, lu, lu)
+        A.data.uniform_(-1.0, 1.0, generator=g)
+        x = torch.randn(N_GBMV, dtype=dt, device=dev, generator=g)
+        y = torch.empty(N_GBMV, dtype=dt, device=dev)
+        gb.append((f"gbmv_{dt_name}_l{lu}", A, x, y, gbmv_bytes(N_GBMV, lu, lu, A.data.element_size())))
+    mm = []
+    if hasattr(bm, "banded_mul_"):
+        for dt_name in ("f32", "f64"):
+            dt = torch.float32 if dt_name == "f32" else torch.float64
+            A = bm.BandedMatrix(bm.band_storage(33, N_GBMM, dt, dev), N_GBMM, 16, 16)
+            B = bm.BandedMatrix(bm.band_storage(33, N_GBMM, dt, dev), N_GBMM, 16, 16)
+            A.data.uniform_(-1.0, 1.0, generator=g)
+            B.data.uniform_(-1.0, 1.0, generator=g)
+            C = bm.BandedMatrix(bm.band_storage(65, N_GBMM, dt, dev), N_GBMM, 32, 32)
+            mm.append((f"gbmm_{dt_name}_l16", A, B, C, gbmm_bytes(N_GBMM, 16, 16, A.data.element_size())))
+
+    n_launch = len(gb) + len(mm)
+    ev = {lab: [] for lab, *_ in gb + mm}
+
+    def step(record):
+        for lab, A, x, y, nb in gb:
+            if record:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            bm.gbmv("N", 1.0, A, x, 0.0, y)
+            if record:
+                e1.record(stream)
+                ev[lab].append((e0, e1))
+        for lab, A, B, C, nb in mm:
+            if record:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            bm.banded_mul_(C, A, B, 1.0, 0.0)
+            if record:
+                e1.record(stream)
+                ev[lab].append((e0, e1))
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler(dev.index) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    if world > 1:
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(tt.item())
+    step_bytes = sum(c[-1] for c in gb + mm)
+    value = world * step_bytes * args.steps / (ms / 1e3) / 1e9
+
+    per_case = []
+    for lab, *rest in gb + mm:
+        nb = rest[-1]
+        t_ms = statistics.mean(a.elapsed_time(b) for a, b in ev[lab])
+        per_case.append({"case": lab, "GBps": nb / (t_ms / 1e3) / 1e9, "ms": t_ms, "bytes": nb})
+    peak, peak_kind = _peaks()
+    for c in per_case:
+        c["frac_of_hbm"] = c["GBps"] / peak
+    dom = max(per_case, key=lambda c: c["ms"])
+    traffic = _traffic(dom["case"])
+
+    # e2e through the public API with host buffers
+    e2e = None
+    if rank == 0 or world > 1:
+        e2e = run_e2e(bm, gb, mm, dev, stream, max(1, min(args.steps, 3)))
+    out = None
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (torch Philox, seeded)",
+            "config": {"workload": WORKLOAD, "l2": "every operand set > 129 MB L2 (no flush needed)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "kernel": dom["case"], "achieved": dom["GBps"], "peak": peak,
+                         "unit": "GB/s", "frac": dom["GBps"] / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs"},
+            "sweep": per_case,
+            "e2e": e2e,
+            "gpu_launches": n_launch * args.steps,
+            "clocks": clk.summary(),
+        }
+    return out
+
+
+def run_e2e(bm, gb, mm, dev, stream, steps):
+    """Same step through the public API with pinned host inputs/outputs; copies are timed."""
+    import torch
+
+    host = []
+    h2d = d2h = 0
+    for lab, A, x, y, nb in gb:
+        hA = torch.empty(A.data.shape[1], A.lda, dtype=A.dtype, pin_memory=True)
+        hA.copy_(A.data.t())
+        hx = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+        hx.copy_(x)
+        hy = torch.empty(y.shape, dtype=y.dtype, pin_memory=True)
+        host.append(("gbmv", A, hA, x, hx, y, hy, nb))
+        h2d += hA.numel() * hA.element_size() + hx.numel() * hx.element_size()
+        d2h += hy.numel() * hy.element_size()
+    for lab, A, B, C, nb in mm:
+        hA = torch.empty(A.data.shape[1], A.lda, dtype=A.dtype, pin_memory=True)
+        hA.copy_(A.data.t())
+        hB = torch.empty(B.data.shape[1], B.lda, dtype=B.dtype, pin_memory=True)
+        hB.copy_(B.data.t())
+        hC = torch.empty(C.data.shape[1], C.lda, dtype=C.dtype, pin_memory=True)
+        host.append(("gbmm", A, hA, B, hB, C, hC, nb))
+        h2d += 2 * hA.numel() * hA.element_size()
+        d2h += hC.numel() * hC.element_size()
+    nbytes = sum(h[-1] for h in host)
+
+    def step():
+        for kind, A, hA, X, hX, Y, hY, nb in host:
+            A.data.t().copy_(hA, non_blocking=True)
+            if kind == "gbmv":
+                X.copy_(hX, non_blocking=True)
+                bm.gbmv("N", 1.0, A, X, 0.0, Y)
+                hY.copy_(Y, non_blocking=True)
+            else:
+                X.data.t().copy_(hX, non_blocking=True)
+                bm.banded_mul_(Y, A, X, 1.0, 0.0)
+                hY.copy_(Y.data.t(), non_blocking=True)
+
+    step()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    return {"value": nbytes / (ms / 1e3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_sweep(max(1, min(args.steps, 3)), min(args.warmup, 1))
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["sec_per_step"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (numpy PCG64)", "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
+                             "sample": cb["sample"], "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"]},
+            "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            cb = cpu_sweep(1, 1)
+            out["cpu_baseline"] = {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
+                                   "sample": cb["sample"], "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"]}
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
