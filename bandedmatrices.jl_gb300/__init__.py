@@ -11,11 +11,13 @@ from . import _lib
 from ._lib import BandedGPUError
 from .banded import (BandedMatrix, BandError, DimensionMismatch, band_storage, bandeddata, bandwidth, bandwidths,
                      brand, brandn, gbmv)
+from .gbmm import banded_mul, banded_mul_, gbmm, nonzero_bands, prodbandwidths
 from .linalg import ldiv, mul, mul_, mul_t_
 
 __all__ = [
     "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
+    "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
 ]
 
 

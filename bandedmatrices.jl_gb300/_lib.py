@@ -32,6 +32,10 @@ SIGNATURES: dict[str, list] = {
     "bm_device_status": [P, I, P],
     "bm_dgbmv": [C, i64, i64, i64, i64, D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmv": [C, i64, i64, i64, i64, F, P, i64, P, i64, F, P, i64, P],
+    "bm_dgbmm": [i64] * 9 + [D, P, i64, P, i64, D, P, i64, P],
+    "bm_sgbmm": [i64] * 9 + [F, P, i64, P, i64, F, P, i64, P],
+    "bm_dgb_nonzero_bands": [i64, i64, i64, i64, P, i64, P, P],
+    "bm_sgb_nonzero_bands": [i64, i64, i64, i64, P, i64, P, P],
 }
 
 

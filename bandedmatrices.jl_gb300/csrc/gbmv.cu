@@ -18,6 +18,9 @@
 //        y_j = fma(alpha, t, beta*y_j).
 //
 // Roofline: HBM.  Algorithmic bytes per call = s*(lda*n + |x| + |y|*(beta!=0 ? 2 : 1)).
+#include <cstdio>
+#include <cstdlib>
+
 #include "common.cuh"
 
 namespace bm {
@@ -99,7 +102,7 @@ __device__ __forceinline__ void issue_tile(const GbmvParams<T>& p, unsigned char
 }
 
 template <typename T, bool TRANS>
-__global__ void __launch_bounds__(256) gbmv_tma_kernel(const GbmvParams<T> p) {
+__global__ void __launch_bounds__(512) gbmv_tma_kernel(const GbmvParams<T> p) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
   unsigned char* slots = smem + 128;
@@ -143,33 +146,98 @@ __global__ void __launch_bounds__(256) gbmv_tma_kernel(const GbmvParams<T> p) {
     }
     __syncthreads();
 
+    // Tile-local 32-bit indexing.  For 'N', outputs are rows i and A's columns are
+    // local to c0; for 'T', outputs are columns j and x's rows are local to x0.
+    const int nout = (int)(o1 - o0);
+    const int lda = (int)p.lda, kl = (int)p.kl, ku = (int)p.ku, kb = kl + ku + 1;
+    const int bd = blockDim.x;
     if (!TRANS) {
-      for (i64 i = o0 + threadIdx.x; i < o1; i += blockDim.x) {
-        const i64 jlo = max((i64)0, i - p.kl), jhi = min(p.n - 1, i + p.ku);
-        T acc = (p.beta == T(0)) ? T(0) : p.beta * p.y[i];
-        int ia = (int)(jlo * p.lda + p.ku + i - jlo - ra.gs);
-        int ix = (int)(jlo - rx.gs);
-        const int step = (int)p.lda - 1;
-        for (i64 j = jlo; j <= jhi; ++j) {
-          acc = fma(sx[ix], sa[ia], acc);
-          ia += step;
-          ++ix;
+      const int abase = (int)(c0 * p.lda - ra.gs) + ku;  // + jj*(lda-1) + li
+      const int xbase = (int)(c0 - rx.gs);               // + jj
+      const i64 nmax = p.n - 1 - c0;                     // last local column
+      const int off = (int)(o0 - c0);                    // local index of row o0
+      for (int t = threadIdx.x; t < nout; t += 2 * bd) {
+        const int t2 = t + bd;
+        const int li = off + t, li2 = off + t2;
+        const bool two = t2 < nout;
+        const bool full1 = (o0 + t - kl >= 0) && (li + ku <= nmax);
+        const bool full2 = two && (o0 + t2 - kl >= 0) && (li2 + ku <= nmax);
+        T acc1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t];
+        T acc2 = (two && p.beta != T(0)) ? p.beta * p.y[o0 + t2] : T(0);
+        if (full1 && full2) {
+          // two independent chains over all kb terms
+          int ia = abase + (li - kl) * (lda - 1) + li, ix = xbase + li - kl;
+          int ia2 = ia + bd * lda, ix2 = ix + bd;
+#pragma unroll 4
+          for (int q = 0; q < kb; ++q) {
+            acc1 = fma(sx[ix], sa[ia], acc1);
+            acc2 = fma(sx[ix2], sa[ia2], acc2);
+            ia += lda - 1; ia2 += lda - 1; ++ix; ++ix2;
+          }
+        } else {
+          {
+            const int jlo = (int)max((i64)(li - kl), -c0), jhi = (int)min((i64)(li + ku), nmax);
+            int ia = abase + jlo * (lda - 1) + li, ix = xbase + jlo;
+            for (int jj = jlo; jj <= jhi; ++jj) {
+              acc1 = fma(sx[ix], sa[ia], acc1);
+              ia += lda - 1; ++ix;
+            }
+          }
+          if (two) {
+            const int jlo = (int)max((i64)(li2 - kl), -c0), jhi = (int)min((i64)(li2 + ku), nmax);
+            int ia = abase + jlo * (lda - 1) + li2, ix = xbase + jlo;
+            for (int jj = jlo; jj <= jhi; ++jj) {
+              acc2 = fma(sx[ix], sa[ia], acc2);
+              ia += lda - 1; ++ix;
+            }
+          }
         }
-        p.y[i] = acc;
+        p.y[o0 + t] = acc1;
+        if (two) p.y[o0 + t2] = acc2;
       }
     } else {
-      for (i64 j = o0 + threadIdx.x; j < o1; j += blockDim.x) {
-        const i64 ilo = max((i64)0, j - p.ku), ihi = min(p.m - 1, j + p.kl);
-        T acc = T(0);
-        int ia = (int)(j * p.lda + p.ku + ilo - j - ra.gs);
-        int ix = (int)(ilo - rx.gs);
-        for (i64 i = ilo; i <= ihi; ++i) {
-          acc = fma(sa[ia], sx[ix], acc);
-          ++ia;
-          ++ix;
+      const int abase = (int)(o0 * p.lda - ra.gs) + ku;  // + lj*lda + (li - lj) with li local to o0
+      const int xbase = (int)(o0 - rx.gs);               // + li
+      const i64 mmax = p.m - 1 - o0;
+      for (int t = threadIdx.x; t < nout; t += 2 * bd) {
+        const int t2 = t + bd;
+        const bool two = t2 < nout;
+        const bool full1 = (o0 + t - ku >= 0) && (t + kl <= mmax);
+        const bool full2 = two && (o0 + t2 - ku >= 0) && (t2 + kl <= mmax);
+        T acc1 = T(0), acc2 = T(0);
+        if (full1 && full2) {
+          int ia = abase + t * lda - ku, ix = xbase + t - ku;
+          int ia2 = ia + bd * lda, ix2 = ix + bd;
+#pragma unroll 4
+          for (int q = 0; q < kb; ++q) {
+            acc1 = fma(sa[ia], sx[ix], acc1);
+            acc2 = fma(sa[ia2], sx[ix2], acc2);
+            ++ia; ++ia2; ++ix; ++ix2;
+          }
+        } else {
+          {
+            const int ilo = (int)max((i64)(t - ku), -o0), ihi = (int)min((i64)(t + kl), mmax);
+            int ia = abase + t * lda + ilo - t, ix = xbase + ilo;
+            for (int li = ilo; li <= ihi; ++li) {
+              acc1 = fma(sa[ia], sx[ix], acc1);
+              ++ia; ++ix;
+            }
+          }
+          if (two) {
+            const int ilo = (int)max((i64)(t2 - ku), -o0), ihi = (int)min((i64)(t2 + kl), mmax);
+            int ia = abase + t2 * lda + ilo - t2, ix = xbase + ilo;
+            for (int li = ilo; li <= ihi; ++li) {
+              acc2 = fma(sa[ia], sx[ix], acc2);
+              ++ia; ++ix;
+            }
+          }
         }
-        const T y0 = (p.beta == T(0)) ? T(0) : p.beta * p.y[j];
-        p.y[j] = fma(p.alpha, acc, y0);
+        const T y1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t];
+        p.y[o0 + t] = fma(p.alpha, acc1, y1);
+        if (two) {
+          const T y2 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t2];
+          p.y[o0 + t2] = fma(p.alpha, acc2, y2);
+        }
       }
     }
     fence_proxy_async_smem();
@@ -232,7 +300,44 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   const int nsm = num_sms();
 
   const bool aligned = ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(x)) & 15) == 0;
-  if (incx != 1 || incy != 1 || !aligned || alpha == T(0) || (lda * n) >= ((i64)1 << 40)) {
+  const i64 s = sizeof(T);
+  const i64 halo = kl + ku;
+  const i64 per_out = (lda + 1) * s;  // bytes of A plus x per band column
+
+  // Tile selection: a ring of `stages` slots per CTA, `ctas` CTAs per SM.
+  // BM_GBMV_CFG="ctas,stages,kbytes_per_cta" overrides the search (tuning).
+  int ctas = 1, stages = 0;
+  i64 tile = 0, budget = 220 * 1024;
+  if (const char* env = getenv("BM_GBMV_CFG")) {
+    int c = 0, st = 0, kb = 0;
+    if (sscanf(env, "%d,%d,%d", &c, &st, &kb) == 3 && c >= 1 && c <= 4 && st >= 2 && st <= 8 && kb >= 16 &&
+        kb <= 224) {
+      ctas = c;
+      stages = st;
+      budget = (i64)kb * 1024;
+    }
+  }
+  auto tile_for = [&](int st) {
+    const i64 slot = budget / st;
+    const i64 cols = (slot - 384) / per_out;
+    return notr ? cols - halo : cols - (halo * s + per_out - 1) / per_out;
+  };
+  if (!stages) {
+    // Measured on GB300 (n = 2^24 sweep): two large ring slots beat deeper rings of
+    // smaller tiles; two CTAs per SM pay off for narrow bands, one for wide ones.
+    stages = 2;
+    if (halo <= 16) {
+      ctas = 2;
+      budget = 110 * 1024;
+    }
+  }
+  tile = tile_for(stages);
+  tile = std::min<i64>(tile, 8192);
+  const i64 want = ceil_div(leny, (i64)nsm * ctas * 2);  // >= ~2 tiles per CTA on small problems
+  if (want < tile) tile = std::min<i64>(tile, std::max<i64>(64, ((want + 63) / 64) * 64));
+
+  if (incx != 1 || incy != 1 || !aligned || alpha == T(0) || tile < 32 || (lda * n) >= ((i64)1 << 40)) {
+    // Generic path: any strides / alignment, or a band too wide for a staged tile.
     const int threads = 256;
     const i64 blocks = std::min<i64>(ceil_div(leny, threads), (i64)nsm * 32);
     if (notr)
@@ -244,26 +349,6 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
     return launch_status(name);
   }
 
-  // Tile selection: a ring of `stages` slots inside ~200 KB of shared memory.
-  const i64 s = sizeof(T);
-  const i64 budget = 200 * 1024;
-  const i64 halo = kl + ku;
-  const i64 per_out = (lda + 1) * s;  // bytes of A plus x per column
-  int stages = 4;
-  i64 tile = 0;
-  for (int st = 4; st >= 2; --st) {
-    const i64 slot = budget / st;
-    const i64 cols = (slot - 256) / per_out;
-    const i64 tl = notr ? cols - halo : cols - (halo * s + per_out - 1) / per_out;
-    stages = st;
-    tile = tl;
-    if (tl >= 4 * halo && tl >= 256) break;
-  }
-  if (tile < 32) return BM_ERR_UNSUPPORTED;  // band too wide for one slot; not reached for lda <= 2000
-  tile = std::min<i64>(tile, 4096);
-  // Keep at least ~2 tiles per CTA when the problem is small.
-  const i64 want = ceil_div(leny, (i64)nsm * 2);
-  if (want < tile) tile = std::max<i64>(32, ((want + 31) / 32) * 32);
   GbmvParams<T> p;
   p.m = m; p.n = n; p.kl = kl; p.ku = ku; p.lda = lda;
   p.alpha = alpha; p.beta = beta; p.A = A; p.x = x; p.y = y;
@@ -271,21 +356,25 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   p.ntiles = ceil_div(leny, tile);
   p.stages = stages;
   const i64 cols = notr ? tile + halo : tile;
-  const i64 xlen = notr ? tile + halo : tile + halo;
+  const i64 xlen = tile + halo;
   const i64 abytes = ((cols * lda + 2 * (16 / s)) * s + 127) / 128 * 128;
   const i64 xbytes = ((xlen + 2 * (16 / s)) * s + 127) / 128 * 128;
   p.xoff = (uint32_t)abytes;
   p.stage_bytes = (uint32_t)(abytes + xbytes);
   p.status = status_word();
   const int smem = 128 + stages * (int)p.stage_bytes;
+  if (smem > 227 * 1024) {
+    set_error("%s: internal tile selection exceeded shared memory (%d bytes)", name, smem);
+    return BM_ERR_UNSUPPORTED;
+  }
   const void* kfn = notr ? (const void*)gbmv_tma_kernel<T, false> : (const void*)gbmv_tma_kernel<T, true>;
   int r = cuda_status(ensure_smem(kfn, smem), name);
   if (r) return r;
-  const i64 grid = std::min<i64>(p.ntiles, nsm);
+  const i64 grid = std::min<i64>(p.ntiles, (i64)nsm * ctas);
   if (notr)
-    gbmv_tma_kernel<T, false><<<(unsigned)grid, 256, smem, stream>>>(p);
+    gbmv_tma_kernel<T, false><<<(unsigned)grid, 512, smem, stream>>>(p);
   else
-    gbmv_tma_kernel<T, true><<<(unsigned)grid, 256, smem, stream>>>(p);
+    gbmv_tma_kernel<T, true><<<(unsigned)grid, 512, smem, stream>>>(p);
   return launch_status(name);
 }
 

@@ -60,6 +60,30 @@ int bm_sgbmv(char trans, int64_t m, int64_t n, int64_t kl, int64_t ku, float alp
              int64_t lda, const float *x, int64_t incx, float beta, float *y, int64_t incy,
              bm_stream_t stream);
 
+/* ------------------------------------------------------------------ gbmm
+ * C <- alpha*A*B + beta*C for banded A (n x nu, bandwidths (Al,Au)), B (nu x m,
+ * (Bl,Bu)) and C (n x m, (Cl,Cu)), all bandwidths >= 0 and C's band wide enough
+ * for every in-matrix nonzero of A*B: Cl >= min(Al+Bl, n-1), Cu >= min(Au+Bu, m-1).
+ * Bands of C beyond the product are scaled by beta; beta == 0 means C is not read.
+ * Replaces gbmm!/_gbmm! (src/banded/gbmm.jl:207-340), reached from A*B and
+ * mul!(C,A,B,alpha,beta) (materialize!, src/generic/matmul.jl:177-189); each C
+ * entry equals the column dgbmv of _gbmm! bit for bit. */
+int bm_dgbmm(int64_t n, int64_t nu, int64_t m, int64_t Al, int64_t Au, int64_t Bl, int64_t Bu, int64_t Cl,
+             int64_t Cu, double alpha, const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+             double *C, int64_t ldc, bm_stream_t stream);
+int bm_sgbmm(int64_t n, int64_t nu, int64_t m, int64_t Al, int64_t Au, int64_t Bl, int64_t Bu, int64_t Cl,
+             int64_t Cu, float alpha, const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+             float *C, int64_t ldc, bm_stream_t stream);
+
+/* flags[r] <- 1 if band r (storage row r) of the m x n band matrix (l,u) holds a
+ * nonzero in-matrix entry, else 0 (flags: l+u+1 device ints).  The device side of
+ * _num_zeroband_u/_num_zeroband_l (src/banded/gbmm.jl:191-205), which gbmm! uses
+ * to accept a C narrower than the product. */
+int bm_dgb_nonzero_bands(int64_t m, int64_t n, int64_t l, int64_t u, const double *A, int64_t lda, int *flags,
+                         bm_stream_t stream);
+int bm_sgb_nonzero_bands(int64_t m, int64_t n, int64_t l, int64_t u, const float *A, int64_t lda, int *flags,
+                         bm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
