@@ -13,11 +13,14 @@ from .banded import (BandedMatrix, BandError, DimensionMismatch, band_storage, b
                      brand, brandn, gbmv)
 from .gbmm import banded_mul, banded_mul_, gbmm, nonzero_bands, prodbandwidths
 from .linalg import ldiv, mul, mul_, mul_t_
+from .lu import BandedLU, ldiv_, lu, lu_, transpose
+from .batched import BandedBatch, lpt_order
 
 __all__ = [
     "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
+    "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order",
 ]
 
 

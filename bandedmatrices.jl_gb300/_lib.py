@@ -36,7 +36,16 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbmm": [i64] * 9 + [F, P, i64, P, i64, F, P, i64, P],
     "bm_dgb_nonzero_bands": [i64, i64, i64, i64, P, i64, P, P],
     "bm_sgb_nonzero_bands": [i64, i64, i64, i64, P, i64, P, P],
+    "bm_dgbtrf": [i64, i64, i64, i64, P, i64, P, P, P],
+    "bm_sgbtrf": [i64, i64, i64, i64, P, i64, P, P, P],
+    "bm_dgbtrs": [C, i64, i64, i64, i64, P, i64, P, P, i64, P],
+    "bm_sgbtrs": [C, i64, i64, i64, i64, P, i64, P, P, i64, P],
+    "bm_dgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
+    "bm_sgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
 }
+
+# bm_gb_desc as a numpy structured dtype (9 x int64, C layout)
+DESC_FIELDS = ["n", "kl", "ku", "nrhs", "ab_offset", "ldab", "b_offset", "ldb", "ipiv_offset"]
 
 
 class BandedGPUError(RuntimeError):

@@ -1,0 +1,87 @@
+"""Batched banded solves: thousands of independent systems of uneven n, (kl, ku)
+and right-hand-side counts in one persistent launch (bm_{d,s}gbsv_batched).
+
+The batch owns three flat device buffers -- every system's gbtrf band storage,
+right-hand sides and pivots -- plus a device descriptor table.  Systems are
+handed to warps from a device work queue in longest-processing-time order (cost
+n*kl*(kl+ku), largest first) so that the tail of the launch stays short.  The
+launch performs no allocation and no host synchronisation, so a whole solve can
+be captured once in a CUDA graph and replayed.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .banded import BandedMatrix, _prefix, _ptr, _stream
+
+
+def lpt_order(n, kl, ku, nrhs) -> np.ndarray:
+    """System indices, most expensive first (factor + solve flop estimate)."""
+    n, kl, ku, nrhs = (np.asarray(v, dtype=np.int64) for v in (n, kl, ku, nrhs))
+    cost = n * (2 * kl * (kl + ku) + kl) + nrhs * 2 * n * (2 * kl + ku + 1)
+    return np.argsort(-cost, kind="stable").astype(np.int32)
+
+
+class BandedBatch:
+    """A batch of square banded systems A_s x_s = b_s with device-resident storage."""
+
+    def __init__(self, n, kl, ku, nrhs, dtype=torch.float64, device="cuda"):
+        self.count = len(n)
+        self.n = np.asarray(n, dtype=np.int64)
+        self.kl = np.asarray(kl, dtype=np.int64)
+        self.ku = np.asarray(ku, dtype=np.int64)
+        self.nrhs = np.asarray(nrhs, dtype=np.int64)
+        self.dtype, self.device = dtype, torch.device(device)
+        self.ldab = 2 * self.kl + self.ku + 1
+        self.ab_off = np.concatenate([[0], np.cumsum(self.ldab * self.n)[:-1]]).astype(np.int64)
+        self.b_off = np.concatenate([[0], np.cumsum(self.n * self.nrhs)[:-1]]).astype(np.int64)
+        self.ip_off = np.concatenate([[0], np.cumsum(self.n)[:-1]]).astype(np.int64)
+        self.AB = torch.zeros(int((self.ldab * self.n).sum()), dtype=dtype, device=self.device)
+        self.B = torch.zeros(int((self.n * self.nrhs).sum()), dtype=dtype, device=self.device)
+        self.ipiv = torch.zeros(int(self.n.sum()), dtype=torch.int64, device=self.device)
+        self.info = torch.zeros(self.count, dtype=torch.int64, device=self.device)
+        desc = np.stack([self.n, self.kl, self.ku, self.nrhs, self.ab_off, self.ldab, self.b_off, self.n,
+                         self.ip_off], axis=1).astype(np.int64)
+        self.descs = torch.from_numpy(np.ascontiguousarray(desc)).to(self.device)
+        self.order = torch.from_numpy(lpt_order(self.n, self.kl, self.ku, self.nrhs)).to(self.device)
+        self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.max_kl = int(self.kl.max()) if self.count else 0
+        self.max_ku = int(self.ku.max()) if self.count else 0
+
+    # -- views of one system's storage -------------------------------------------------
+    def band(self, s: int) -> BandedMatrix:
+        """System s's gbtrf storage as a BandedMatrix with bandwidths (kl, kl+ku)."""
+        n, ld, off = int(self.n[s]), int(self.ldab[s]), int(self.ab_off[s])
+        data = self.AB[off: off + ld * n].view(n, ld).t()
+        return BandedMatrix(data, n, int(self.kl[s]), int(self.kl[s] + self.ku[s]))
+
+    def matrix_band(self, s: int) -> torch.Tensor:
+        """System s's (kl+ku+1) x n band of A inside its gbtrf storage (rows kl..)."""
+        return self.band(s).data[int(self.kl[s]):, :]
+
+    def rhs(self, s: int) -> torch.Tensor:
+        n, k, off = int(self.n[s]), int(self.nrhs[s]), int(self.b_off[s])
+        return self.B[off: off + n * k].view(k, n).t()
+
+    def pivots(self, s: int) -> torch.Tensor:
+        off = int(self.ip_off[s])
+        return self.ipiv[off: off + int(self.n[s])]
+
+    # -- the launch ---------------------------------------------------------------------
+    def factor_solve(self, stream=None) -> None:
+        """Factor every system in place and overwrite its right-hand sides with the solution."""
+        st = ctypes.c_void_p(stream) if stream is not None else _stream(self.device)
+        _lib.call(f"bm_{_prefix(self.dtype)}gbsv_batched", self.count, _ptr(self.descs), _ptr(self.order),
+                  _ptr(self.AB), _ptr(self.ipiv), _ptr(self.B), _ptr(self.info), _ptr(self.counter), self.max_kl,
+                  self.max_ku, st)
+
+    def capture(self) -> torch.cuda.CUDAGraph:
+        """Capture factor_solve in a CUDA graph (call once eagerly first for device set-up)."""
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.factor_solve()
+        return g

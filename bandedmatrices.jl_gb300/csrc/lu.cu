@@ -1,0 +1,173 @@
+// Banded LU entry points: xGBTRF / xGBTRS for one system and the batched
+// persistent factor+solve.  The device algorithms are in lu.cuh.
+//
+// Replaces LAPACK.gbtrf! (lu!, src/banded/BandedLU.jl:90-103) and LAPACK.gbtrs!
+// (ldiv!, src/banded/linalg.jl:24-30 'N', :41-47 'T').
+#include "lu.cuh"
+
+namespace bm {
+
+constexpr int kP = 4;  // rows staged ahead by cp.async in gbtrf
+
+template <typename T>
+__global__ void __launch_bounds__(32) gbtrf_one_kernel(i64 m, i64 n, int kl, int ku, T* ab, i64 ldab, i64* ipiv,
+                                                       i64* info) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const i64 r = gbtrf_warp<T, kP>(m, n, kl, ku, ab, ldab, ipiv, reinterpret_cast<T*>(smem_raw));
+  if (threadIdx.x == 0) *info = r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) gbtrs_one_kernel(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* ab,
+                                                       i64 ldab, const i64* ipiv, T* B, i64 ldb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (i64 r = blockIdx.x; r < nrhs; r += gridDim.x)
+    gbtrs_warp<T>(trans, n, kl, ku, ab, ldab, ipiv, B + r * ldb, reinterpret_cast<T*>(smem_raw));
+}
+
+// Persistent batched factor + solve.  Each warp takes the next system from a
+// device work queue (an atomic counter over `order`, which lists systems from the
+// most to the least expensive), factors it in place and solves its right-hand
+// sides.  Shared memory per warp is sized for the widest band of the batch.
+template <typename T>
+__global__ void __launch_bounds__(128) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
+                                                           const int32_t* __restrict__ order, T* AB, i64* ipiv,
+                                                           T* B, i64* info, int32_t* counter, i64 warp_elems) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* smem = reinterpret_cast<T*>(smem_raw) + warp * warp_elems;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(counter, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= count) break;
+    const int s = order ? order[idx] : idx;
+    const bm_gb_desc d = descs[s];
+    T* ab = AB + d.ab_offset;
+    i64* ip = ipiv + d.ipiv_offset;
+    const i64 r = gbtrf_warp<T, kP>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
+    if (lane == 0) info[s] = r;
+    __syncwarp();
+    if (r == 0)
+      for (i64 c = 0; c < d.nrhs; ++c)
+        gbtrs_warp<T>(false, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, B + d.b_offset + c * d.ldb, smem);
+    __syncwarp();
+  }
+}
+
+template <typename T>
+static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
+                      const char* name) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (kl < 0) return -3;
+  if (ku < 0) return -4;
+  if (ldab < 2 * kl + ku + 1) return -6;
+  if (!info) return -8;
+  if (m == 0 || n == 0) return cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
+  if (!ipiv) return -7;
+  const i64 bytes = gbtrf_smem_elems<kP>((int)kl, (int)ku) * (i64)sizeof(T);
+  if (bytes > 227 * 1024) {
+    set_error("%s: band (kl=%lld, ku=%lld) exceeds the single-system window limit", name, (long long)kl,
+              (long long)ku);
+    return BM_ERR_UNSUPPORTED;
+  }
+  int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T>, (int)bytes), name);
+  if (r) return r;
+  gbtrf_one_kernel<T><<<1, 32, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+  return launch_status(name);
+}
+
+template <typename T>
+static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, i64 ldab, const i64* ipiv, T* B,
+                      i64 ldb, cudaStream_t stream, const char* name) {
+  const bool notr = (trans == 'N' || trans == 'n');
+  if (!notr && !(trans == 'T' || trans == 't' || trans == 'C' || trans == 'c')) return -1;
+  if (n < 0) return -2;
+  if (kl < 0) return -3;
+  if (ku < 0) return -4;
+  if (nrhs < 0) return -5;
+  if (ldab < 2 * kl + ku + 1) return -7;
+  if (ldb < std::max<i64>(1, n)) return -10;
+  if (n == 0 || nrhs == 0) return BM_OK;
+  const i64 bytes = gbtrs_smem_elems((int)kl, (int)ku) * (i64)sizeof(T);
+  if (bytes > 227 * 1024) {
+    set_error("%s: band too wide for the staged solve", name);
+    return BM_ERR_UNSUPPORTED;
+  }
+  int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T>, (int)bytes), name);
+  if (r) return r;
+  const i64 grid = std::min<i64>(nrhs, 65535);
+  gbtrs_one_kernel<T><<<(unsigned)grid, 32, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab, ipiv,
+                                                                   B, ldb);
+  return launch_status(name);
+}
+
+template <typename T>
+static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* order, T* AB, i64* ipiv, T* B,
+                             i64* info, int32_t* counter, i64 max_kl, i64 max_ku, cudaStream_t stream,
+                             const char* name) {
+  if (count < 0) return -1;
+  if (!descs && count) return -2;
+  if (max_kl < 0) return -10;
+  if (max_ku < 0) return -11;
+  if (!counter) return -9;
+  if (count == 0) return BM_OK;
+  const i64 welems = std::max(gbtrf_smem_elems<kP>((int)max_kl, (int)max_ku), gbtrs_smem_elems((int)max_kl, (int)max_ku));
+  const i64 wbytes = ((welems * (i64)sizeof(T) + 15) / 16) * 16;
+  const i64 welems_aligned = wbytes / (i64)sizeof(T);
+  if (wbytes > 227 * 1024) {
+    set_error("%s: widest band of the batch exceeds the per-warp window limit", name);
+    return BM_ERR_UNSUPPORTED;
+  }
+  // warps per CTA: as many as fit in ~100 KB (two CTAs per SM), at most 4
+  int wpc = (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
+  const int smem = (int)(wpc * wbytes);
+  int r = cuda_status(ensure_smem((const void*)gbsv_batched_kernel<T>, smem), name);
+  if (r) return r;
+  int per_sm = 0;
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gbsv_batched_kernel<T>, 32 * wpc, smem), name);
+  if (r) return r;
+  per_sm = std::max(per_sm, 1);
+  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(count, wpc));
+  r = cuda_status(cudaMemsetAsync(counter, 0, sizeof(int32_t), stream), name);
+  if (r) return r;
+  gbsv_batched_kernel<T><<<(unsigned)grid, 32 * wpc, smem, stream>>>(count, descs, order, AB, ipiv, B, info, counter,
+                                                                     welems_aligned);
+  return launch_status(name);
+}
+
+}  // namespace bm
+
+extern "C" int bm_dgbtrf(int64_t m, int64_t n, int64_t kl, int64_t ku, double* AB, int64_t ldab, int64_t* ipiv,
+                         int64_t* info, bm_stream_t stream) {
+  return bm::gbtrf_impl<double>(m, n, kl, ku, AB, ldab, ipiv, info, reinterpret_cast<cudaStream_t>(stream),
+                                "bm_dgbtrf");
+}
+extern "C" int bm_sgbtrf(int64_t m, int64_t n, int64_t kl, int64_t ku, float* AB, int64_t ldab, int64_t* ipiv,
+                         int64_t* info, bm_stream_t stream) {
+  return bm::gbtrf_impl<float>(m, n, kl, ku, AB, ldab, ipiv, info, reinterpret_cast<cudaStream_t>(stream),
+                               "bm_sgbtrf");
+}
+extern "C" int bm_dgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double* AB, int64_t ldab,
+                         const int64_t* ipiv, double* B, int64_t ldb, bm_stream_t stream) {
+  return bm::gbtrs_impl<double>(trans, n, kl, ku, nrhs, AB, ldab, ipiv, B, ldb,
+                                reinterpret_cast<cudaStream_t>(stream), "bm_dgbtrs");
+}
+extern "C" int bm_sgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const float* AB, int64_t ldab,
+                         const int64_t* ipiv, float* B, int64_t ldb, bm_stream_t stream) {
+  return bm::gbtrs_impl<float>(trans, n, kl, ku, nrhs, AB, ldab, ipiv, B, ldb,
+                               reinterpret_cast<cudaStream_t>(stream), "bm_sgbtrs");
+}
+extern "C" int bm_dgbsv_batched(int64_t count, const bm_gb_desc* descs, const int32_t* order, double* AB,
+                                int64_t* ipiv, double* B, int64_t* info, int32_t* counter, int64_t max_kl,
+                                int64_t max_ku, bm_stream_t stream) {
+  return bm::gbsv_batched_impl<double>(count, descs, order, AB, ipiv, B, info, counter, max_kl, max_ku,
+                                       reinterpret_cast<cudaStream_t>(stream), "bm_dgbsv_batched");
+}
+extern "C" int bm_sgbsv_batched(int64_t count, const bm_gb_desc* descs, const int32_t* order, float* AB,
+                                int64_t* ipiv, float* B, int64_t* info, int32_t* counter, int64_t max_kl,
+                                int64_t max_ku, bm_stream_t stream) {
+  return bm::gbsv_batched_impl<float>(count, descs, order, AB, ipiv, B, info, counter, max_kl, max_ku,
+                                      reinterpret_cast<cudaStream_t>(stream), "bm_sgbsv_batched");
+}

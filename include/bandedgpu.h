@@ -84,6 +84,53 @@ int bm_dgb_nonzero_bands(int64_t m, int64_t n, int64_t l, int64_t u, const doubl
 int bm_sgb_nonzero_bands(int64_t m, int64_t n, int64_t l, int64_t u, const float *A, int64_t lda, int *flags,
                          bm_stream_t stream);
 
+/* ------------------------------------------------------------------ LU
+ * Partial-pivot banded LU, LAPACK xGBTRF: AB is the (2kl+ku+1) x n gbtrf storage
+ * (ldab >= 2kl+ku+1; matrix in rows kl..2kl+ku, the top kl rows receive fill-in),
+ * factored in place; ipiv receives min(m,n) 1-based pivots; *info (device) receives
+ * LAPACK's info (0, or i > 0 when U(i,i) is exactly zero).  Factors and pivots equal
+ * unblocked dgbtf2's bit for bit.  Replaces LAPACK.gbtrf! in lu!
+ * (src/banded/BandedLU.jl:90-103), which BandedMatrices.jl calls as
+ * gbtrf!(l, u-l, m, data) on the band re-widened to (l, l+u) by _lu (:108-111). */
+int bm_dgbtrf(int64_t m, int64_t n, int64_t kl, int64_t ku, double *AB, int64_t ldab, int64_t *ipiv, int64_t *info,
+              bm_stream_t stream);
+int bm_sgbtrf(int64_t m, int64_t n, int64_t kl, int64_t ku, float *AB, int64_t ldab, int64_t *ipiv, int64_t *info,
+              bm_stream_t stream);
+
+/* Solve op(A) X = B with the xGBTRF factors, LAPACK xGBTRS (trans 'N' or 'T'/'C');
+ * B is n x nrhs column-major (ldb >= max(1,n)), overwritten with X.  Replaces
+ * LAPACK.gbtrs! in ldiv!(::BandedLU, B) (src/banded/linalg.jl:24-30) and
+ * ldiv!(transpose(F), B) (:41-47, :55-56). */
+int bm_dgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double *AB, int64_t ldab,
+              const int64_t *ipiv, double *B, int64_t ldb, bm_stream_t stream);
+int bm_sgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const float *AB, int64_t ldab,
+              const int64_t *ipiv, float *B, int64_t ldb, bm_stream_t stream);
+
+/* ------------------------------------------------------------------ batched
+ * One square system of a batch: its band (gbtrf storage) at AB + ab_offset, its
+ * right-hand sides at B + b_offset (n x nrhs, leading dim ldb), its pivots at
+ * ipiv + ipiv_offset.  Systems may differ in n, kl, ku and nrhs. */
+typedef struct {
+  int64_t n, kl, ku, nrhs;
+  int64_t ab_offset, ldab;
+  int64_t b_offset, ldb;
+  int64_t ipiv_offset;
+} bm_gb_desc;
+
+/* Factor and solve every system of a batch in one persistent launch: warps take
+ * systems from a device work queue in the order `order` (device int32 list of
+ * system indices, most expensive first; NULL = natural order).  info[s] (device)
+ * receives system s's gbtrf info; systems with info != 0 are not solved.
+ * `counter` is one device int32 of workspace (reset by the call).  max_kl/max_ku
+ * bound the bandwidths in the batch (shared memory is sized from them).  No
+ * allocation, no host synchronisation: the call can be captured in a CUDA graph.
+ * No counterpart in the reference (which solves one system per call); per
+ * system it equals lu! + ldiv! (src/banded/BandedLU.jl:90-103, linalg.jl:24-30). */
+int bm_dgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, double *AB, int64_t *ipiv,
+                     double *B, int64_t *info, int32_t *counter, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
+int bm_sgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, float *AB, int64_t *ipiv,
+                     float *B, int64_t *info, int32_t *counter, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

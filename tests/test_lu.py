@@ -1,0 +1,236 @@
+"""Banded LU on the GPU (bm_{d,s}gbtrf / gbtrs / gbsv_batched) against the oracle.
+
+The factorization reproduces dgbtf2 operation for operation, so factors and pivots
+must equal the oracle's bit for bit; solves likewise ('T' with kl > 16 uses a tree
+reduction and is checked to 1e-12).  Cases follow test/test_bandedlu.jl (5x5 (1,1)
+L/U/p, transposed and multiple right-hand sides, non-square errors, zero sizes) plus
+sweeps over n, kl, ku with and without diagonal dominance (pivoting exercised).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "lapack_golden.npz")
+
+
+def dev_band(bm, data_np, m, l, u, device):
+    rows, n = data_np.shape
+    dt = torch.float64 if data_np.dtype == np.float64 else torch.float32
+    d = bm.band_storage(rows, n, dt, device)
+    if rows * n:
+        d.copy_(torch.from_numpy(np.ascontiguousarray(data_np)))
+    return bm.BandedMatrix(d, m, l, u)
+
+
+def rel(a, b):
+    b = np.asarray(b)
+    s = np.abs(b).max() if b.size else 1.0
+    return float(np.abs(np.asarray(a) - b).max() / (s if s > 0 else 1.0)) if b.size else 0.0
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,l,u,shift", [(1, 0, 0, 0.0), (2, 1, 1, 0.0), (5, 1, 1, 0.0), (50, 2, 3, 0.0),
+                                         (300, 4, 3, 0.0), (300, 4, 3, 10.0), (200, 30, 2, 0.0), (200, 2, 30, 0.0),
+                                         (257, 33, 70, 0.0), (400, 64, 64, 0.0), (1000, 7, 0, 0.0),
+                                         (1000, 0, 7, 0.0), (10000, 4, 3, 10.0), (3000, 16, 16, 0.0)])
+def test_gbtrf_gbtrs_bitexact(bm, gpu, orc, dt, n, l, u, shift):
+    rng = np.random.default_rng(n * 131 + l * 7 + u)
+    data = rng.standard_normal((l + u + 1, n)).astype(dt)
+    data[u, :] += dt(shift)
+    A = dev_band(bm, data, n, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(n, n, l, u, orc.lu_storage(data, n, l, u))
+    assert F.info == info
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv), "pivots differ"
+    got = F.factors.data.cpu().numpy()
+    # compare every in-matrix position of the gbtrf storage (the top l rows hold fill-in)
+    mask = orc.band_to_dense(np.ones_like(LU), n, l, l + u) != 0
+    assert np.array_equal(orc.band_to_dense(got, n, l, l + u)[mask], orc.band_to_dense(LU, n, l, l + u)[mask])
+    for nrhs in (1, 3):
+        b = rng.standard_normal((n, nrhs)).astype(dt)
+        bd = torch.from_numpy(b).to(gpu)
+        xN = F.solve(bd).cpu().numpy()
+        xT = F.T.solve(bd).cpu().numpy()
+        refN = orc.gbtrs("N", n, l, u, LU, ipiv, b)
+        refT = orc.gbtrs("T", n, l, u, LU, ipiv, b)
+        assert np.array_equal(xN, refN, equal_nan=True)
+        if l <= 16:
+            assert np.array_equal(xT, refT, equal_nan=True)
+        else:
+            assert rel(xT, refT) < (1e-12 if dt == np.float64 else 1e-5)
+    xv = F.solve(torch.from_numpy(b[:, 0].copy()).to(gpu)).cpu().numpy()
+    assert np.array_equal(xv, refN[:, 0], equal_nan=True)
+
+
+def test_lu_golden_through_gpu(bm, gpu, orc):
+    """OpenBLAS dgbtrf/dgbtrs outputs (tests/golden) reproduced by the GPU factorization."""
+    g = np.load(GOLD)
+    t = 0
+    while f"lu{t}_dims" in g:
+        n, l, u, nrhs, info = (int(v) for v in g[f"lu{t}_dims"])
+        A = dev_band(bm, g[f"lu{t}_data"], n, l, u, gpu)
+        F = bm.lu(A)
+        assert F.info == info
+        assert np.array_equal(F.ipiv.cpu().numpy(), g[f"lu{t}_ipiv"]), t
+        LU = g[f"lu{t}_LU"]
+        got = F.factors.data.cpu().numpy()
+        mask = orc.band_to_dense(np.ones_like(LU), n, l, l + u) != 0
+        dg, dr = orc.band_to_dense(got, n, l, l + u)[mask], orc.band_to_dense(LU, n, l, l + u)[mask]
+        if l >= 32 and u > 64:   # OpenBLAS uses blocked dgbtrf here; the GPU follows dgbtf2
+            assert rel(dg, dr) < 1e-12
+        else:
+            assert np.array_equal(dg, dr), t
+        bd = torch.from_numpy(g[f"lu{t}_b"]).to(gpu)
+        assert rel(F.solve(bd).cpu().numpy(), g[f"lu{t}_xN"]) < 1e-12
+        assert rel(F.T.solve(bd).cpu().numpy(), g[f"lu{t}_xT"]) < 1e-12
+        t += 1
+
+
+def test_cpu_runnable_case(bm, gpu, orc):
+    """brandn(10000,10000,4,3) + 10I: x = A\\b against OpenBLAS at 1e-12, pivots bit-exact."""
+    g = np.load(GOLD)
+    data, b = g["cfg1_data"], g["cfg1_b"]
+    n, l, u = 10000, 4, 3
+    A = dev_band(bm, data, n, l, u, gpu)
+    x = A.solve(torch.from_numpy(b).to(gpu)).cpu().numpy()
+    assert rel(x, g["cfg1_x"]) < 1e-12
+    F = bm.lu(A)
+    assert np.array_equal(F.ipiv.cpu().numpy(), g["cfg1_ipiv"].astype(np.int64))
+    Ad = orc.band_to_dense(data, n, l, u)
+    assert orc.backward_error(Ad, x, b) < 1e-15
+
+
+def test_reference_small_cases(bm, gpu, orc):
+    """test/test_bandedlu.jl:26-53: L, U, p of a 5x5 (1,1) band against dense LU; solves."""
+    import scipy.linalg
+
+    rng = np.random.default_rng(0)
+    data = rng.uniform(size=(3, 5))
+    A = dev_band(bm, data, 5, 1, 1, gpu)
+    Ad = orc.band_to_dense(data, 5, 1, 1)
+    F = bm.lu(A)
+    P, Lf, Uf = scipy.linalg.lu(Ad)
+    assert np.allclose(F.L @ F.U, Ad[F.p - 1])
+    assert np.allclose(F.U, Uf) and np.allclose(F.L, Lf)
+    pf = np.argmax(P, axis=0) + 1
+    assert np.array_equal(F.p, pf)
+    assert F.issuccess()
+    b = rng.uniform(size=5)
+    bd = torch.from_numpy(b).to(gpu)
+    assert np.allclose(F.solve(bd).cpu().numpy(), np.linalg.solve(Ad, b))
+    assert np.allclose(F.T.solve(bd).cpu().numpy(), np.linalg.solve(Ad.T, b))
+    assert np.allclose(F.adjoint().solve(bd).cpu().numpy(), np.linalg.solve(Ad.T, b))
+    # b not overwritten by A \ b
+    b0 = bd.clone()
+    A.solve(bd)
+    assert torch.equal(bd, b0)
+    # multiple right-hand sides (a row-major (5,10) tensor: the call works on a copy)
+    B = torch.from_numpy(rng.uniform(size=(5, 10))).to(gpu)
+    assert np.allclose(F.solve(B).cpu().numpy(), np.linalg.solve(Ad, B.cpu().numpy()))
+    assert np.allclose(bm.ldiv_(F, B.clone()).cpu().numpy(), np.linalg.solve(Ad, B.cpu().numpy()))
+
+
+def test_non_square_and_sizes(bm, gpu, orc):
+    rng = np.random.default_rng(1)
+    for (m, n) in [(7, 5), (5, 7)]:
+        data = rng.uniform(size=(3, n))
+        A = dev_band(bm, data, m, 1, 1, gpu)
+        F = bm.lu(A)
+        LU, ipiv, info = orc.gbtf2(m, n, 1, 1, orc.lu_storage(data, n, 1, 1))
+        assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+        b = torch.from_numpy(rng.uniform(size=m)).to(gpu)
+        with pytest.raises(bm.DimensionMismatch):
+            F.solve(b)
+    F = bm.lu(dev_band(bm, rng.uniform(size=(3, 4)), 5, 1, 1, gpu))
+    assert F.size() == (5, 4) and F.size(1) == 5 and F.size(2) == 4 and F.size(3) == 1
+    with pytest.raises(IndexError):
+        F.size(0)
+    for (shape, bands) in [((0, 0), (1, 1)), ((0, 3), (1, 1)), ((0, 0), (-1, -2))]:
+        A = bm.BandedMatrix.zeros(shape, bands, torch.float64, gpu)
+        F = bm.lu(A)
+        assert F.factors.shape == shape
+        if shape[1] == 0:
+            assert F.solve(torch.zeros(0, dtype=torch.float64, device=gpu)).numel() == 0
+
+
+def test_singular_info(bm, gpu, orc):
+    rng = np.random.default_rng(2)
+    n, l, u = 60, 2, 2
+    data = rng.standard_normal((l + u + 1, n))
+    for r in range(l + u + 1):  # zero out column 20 of A entirely
+        data[r, 20] = 0.0
+    A = dev_band(bm, data, n, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(n, n, l, u, orc.lu_storage(data, n, l, u))
+    assert info > 0 and F.info == info and not F.issuccess()
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_batched_matches_single(bm, gpu, orc, dt):
+    """Uneven batch (n log-uniform, kl/ku uniform in [0,40], 1-4 RHS): every system's
+    factors, pivots and solution equal the single-system oracle's bit for bit."""
+    rng = np.random.default_rng(3)
+    count = 96
+    n = np.exp(rng.uniform(np.log(8), np.log(600), count)).astype(np.int64)
+    kl = rng.integers(0, 41, count)
+    ku = rng.integers(0, 41, count)
+    nrhs = rng.integers(1, 5, count)
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    batch = bm.BandedBatch(n, kl, ku, nrhs, tdt, gpu)
+    datas, rhss = [], []
+    for s in range(count):
+        d = rng.standard_normal((kl[s] + ku[s] + 1, n[s])).astype(dt)
+        d[ku[s], :] += dt(2 * (kl[s] + ku[s]))
+        r = rng.standard_normal((n[s], nrhs[s])).astype(dt)
+        batch.matrix_band(s).copy_(torch.from_numpy(d))
+        batch.rhs(s).copy_(torch.from_numpy(r))
+        datas.append(d)
+        rhss.append(r)
+    batch.factor_solve()
+    torch.cuda.synchronize()
+    info = batch.info.cpu().numpy()
+    for s in range(count):
+        LU, ipiv, inf = orc.gbtf2(n[s], n[s], kl[s], ku[s], orc.lu_storage(datas[s], n[s], kl[s], ku[s]))
+        assert info[s] == inf
+        assert np.array_equal(batch.pivots(s).cpu().numpy(), ipiv)
+        x = orc.gbtrs("N", n[s], kl[s], ku[s], LU, ipiv, rhss[s])
+        assert np.array_equal(batch.rhs(s).cpu().numpy(), x), s
+
+
+def test_batched_graph_replay(bm, gpu):
+    """The batched launch captures into a CUDA graph; replays re-solve refreshed inputs."""
+    rng = np.random.default_rng(4)
+    count = 64
+    n = rng.integers(50, 300, count)
+    kl = rng.integers(1, 20, count)
+    ku = rng.integers(1, 20, count)
+    nrhs = np.ones(count, dtype=np.int64)
+    batch = bm.BandedBatch(n, kl, ku, nrhs, torch.float64, gpu)
+    bands, rhs = [], []
+    for s in range(count):
+        d = rng.standard_normal((kl[s] + ku[s] + 1, n[s]))
+        d[ku[s], :] += 2 * (kl[s] + ku[s])
+        bands.append(torch.from_numpy(d).to(gpu))
+        rhs.append(torch.from_numpy(rng.standard_normal((n[s], 1))).to(gpu))
+
+    def load():
+        batch.AB.zero_()
+        for s in range(count):
+            batch.matrix_band(s).copy_(bands[s])
+            batch.rhs(s).copy_(rhs[s])
+
+    load()
+    batch.factor_solve()
+    torch.cuda.synchronize()
+    ref = batch.B.clone()
+    load()
+    g = batch.capture()
+    for _ in range(2):
+        load()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(batch.B, ref)
