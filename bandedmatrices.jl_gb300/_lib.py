@@ -42,6 +42,7 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbtrs": [C, i64, i64, i64, i64, P, i64, P, P, i64, P],
     "bm_dgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
     "bm_sgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
+    "bm_dgbsv_batched_noalloc": [i64, P, P, P, P, P, i64, i64, P],
 }
 
 # bm_gb_desc as a numpy structured dtype (9 x int64, C layout)

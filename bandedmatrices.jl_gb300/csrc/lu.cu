@@ -3,6 +3,8 @@
 //
 // Replaces LAPACK.gbtrf! (lu!, src/banded/BandedLU.jl:90-103) and LAPACK.gbtrs!
 // (ldiv!, src/banded/linalg.jl:24-30 'N', :41-47 'T').
+#include <mutex>
+
 #include "lu.cuh"
 
 namespace bm {
@@ -137,7 +139,101 @@ static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* 
   return launch_status(name);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free batched solve.  Some callers of this library cannot call
+// cudaMalloc at solve time: code running while a stream is being captured into a
+// CUDA graph, real-time loops that must not block on the allocator, and hosts whose
+// device memory is owned by another runtime's pool (Julia's CUDA.jl, PyTorch) and
+// that cannot hand the library a workspace.  For them, the scratch of the batched
+// solve -- the work-queue counter and the longest-first processing order -- lives
+// in this file-scope device array instead of caller-provided memory.  Every GPU that
+// loads the library keeps these 256 KiB (plus 256 bytes) until the process exits.
+constexpr int kNoAllocMaxSystems = 65536;
+constexpr int kNoAllocHeader = 64;  // int32 slots before the order list; slot 0 = work counter
+static __device__ __align__(256) int32_t g_noalloc_scratch[kNoAllocHeader + kNoAllocMaxSystems];
+
+// Longest-first order of the systems, written to `order`: systems are binned by
+// floor(log2(cost)) (cost as in lpt_order on the host) and emitted from the most
+// expensive bin down.  Within a bin the order is arbitrary; each system's result does
+// not depend on it.  One CTA; count <= kNoAllocMaxSystems.
+__global__ void __launch_bounds__(1024) lpt_order_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
+                                                         int32_t* __restrict__ order) {
+  __shared__ int hist[64];
+  __shared__ int start[64];
+  if (threadIdx.x < 64) hist[threadIdx.x] = 0;
+  __syncthreads();
+  auto bin_of = [&](i64 s) {
+    const bm_gb_desc d = descs[s];
+    const double cost = (double)d.n * (2.0 * d.kl * (d.kl + d.ku) + d.kl) +
+                        2.0 * d.nrhs * d.n * (2.0 * d.kl + d.ku + 1) + 1.0;
+    const int e = ilogb(cost);               // 0 .. 62
+    return 63 - min(max(e, 0), 63);          // most expensive -> bin 0
+  };
+  for (i64 s = threadIdx.x; s < count; s += blockDim.x) atomicAdd(&hist[bin_of(s)], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int b = 0; b < 64; ++b) {
+      start[b] = acc;
+      acc += hist[b];
+    }
+  }
+  __syncthreads();
+  for (i64 s = threadIdx.x; s < count; s += blockDim.x) order[atomicAdd(&start[bin_of(s)], 1)] = (int32_t)s;
+}
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device.
+static int noalloc_scratch(int32_t** out, const char* name) {
+  static std::mutex mu;
+  static int32_t* cache[64] = {nullptr};
+  int dev = 0;
+  int r = cuda_status(cudaGetDevice(&dev), name);
+  if (r) return r;
+  if (dev < 0 || dev >= 64) {
+    set_error("%s: device ordinal %d out of range", name, dev);
+    return BM_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cache[dev]) {
+    int32_t* ptr = nullptr;
+    r = cuda_status(cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch), name);
+    if (r) return r;
+    cache[dev] = ptr;
+  }
+  *out = cache[dev];
+  return BM_OK;
+}
+
+static int gbsv_batched_noalloc_impl(i64 count, const bm_gb_desc* descs, double* AB, i64* ipiv, double* B, i64* info,
+                                     i64 max_kl, i64 max_ku, cudaStream_t stream, const char* name) {
+  if (count < 0) return -1;
+  if (!descs && count) return -2;
+  if (max_kl < 0) return -7;
+  if (max_ku < 0) return -8;
+  if (count > kNoAllocMaxSystems) {
+    set_error("%s: %lld systems exceed the allocation-free limit of %d; use bm_dgbsv_batched", name,
+              (long long)count, kNoAllocMaxSystems);
+    return BM_ERR_UNSUPPORTED;
+  }
+  if (count == 0) return BM_OK;
+  int32_t* scratch = nullptr;
+  int r = noalloc_scratch(&scratch, name);
+  if (r) return r;
+  lpt_order_kernel<<<1, 1024, 0, stream>>>(count, descs, scratch + kNoAllocHeader);
+  r = launch_status(name);
+  if (r) return r;
+  // the batched launch below resets the work counter (scratch[0]) before it starts
+  return gbsv_batched_impl<double>(count, descs, scratch + kNoAllocHeader, AB, ipiv, B, info, scratch, max_kl, max_ku,
+                                   stream, name);
+}
+
 }  // namespace bm
+
+extern "C" int bm_dgbsv_batched_noalloc(int64_t count, const bm_gb_desc* descs, double* AB, int64_t* ipiv, double* B,
+                                        int64_t* info, int64_t max_kl, int64_t max_ku, bm_stream_t stream) {
+  return bm::gbsv_batched_noalloc_impl(count, descs, AB, ipiv, B, info, max_kl, max_ku,
+                                       reinterpret_cast<cudaStream_t>(stream), "bm_dgbsv_batched_noalloc");
+}
 
 extern "C" int bm_dgbtrf(int64_t m, int64_t n, int64_t kl, int64_t ku, double* AB, int64_t ldab, int64_t* ipiv,
                          int64_t* info, bm_stream_t stream) {

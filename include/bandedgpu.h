@@ -131,6 +131,19 @@ int bm_dgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *orde
 int bm_sgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, float *AB, int64_t *ipiv,
                      float *B, int64_t *info, int32_t *counter, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
 
+/* Allocation-free variant of bm_dgbsv_batched, for callers that cannot allocate
+ * device memory when they solve: code running under CUDA stream capture, real-time
+ * loops that must not block on an allocator, and hosts whose device memory belongs
+ * to another runtime's pool.  The caller passes only inputs and outputs; the work
+ * queue and the longest-first order live in a 256 KiB static device array inside
+ * the library, which every GPU that loads the library keeps until exit.  At most
+ * 65536 systems per call (more: BM_ERR_UNSUPPORTED, see bm_last_error()).  The
+ * first call on a device looks up the array's address and should come before any
+ * stream capture.  All calls share the array, so calls that overlap on the GPU
+ * (concurrent streams) race; serialise them.  No counterpart in the reference. */
+int bm_dgbsv_batched_noalloc(int64_t count, const bm_gb_desc *descs, double *AB, int64_t *ipiv, double *B,
+                             int64_t *info, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
