@@ -43,6 +43,7 @@ SIGNATURES: dict[str, list] = {
     "bm_dgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
     "bm_sgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
     "bm_dgbsv_batched_noalloc": [i64, P, P, P, P, P, i64, i64, P],
+    "bm_dsgbsv_batched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, i64, i64, P],
 }
 
 # bm_gb_desc as a numpy structured dtype (9 x int64, C layout)

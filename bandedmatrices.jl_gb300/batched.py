@@ -79,6 +79,32 @@ class BandedBatch:
                   _ptr(self.AB), _ptr(self.ipiv), _ptr(self.B), _ptr(self.info), _ptr(self.counter), self.max_kl,
                   self.max_ku, st)
 
+    def solve_mixed(self, tol: float = 1e-10, maxit: int = 30, stream=None) -> torch.Tensor:
+        """FP32 factorization + FP64-residual iterative refinement (bm_dsgbsv_batched).
+
+        The FP64 band in ``AB`` and the right-hand sides in ``B`` are left untouched; the
+        solutions go to ``X`` (returned), the corrections taken per system to ``iters``
+        and the final backward errors to ``berr``.  Requires a batch of Float64 storage.
+        """
+        if self.dtype != torch.float64:
+            raise TypeError("solve_mixed refines to Float64: build the batch with dtype=torch.float64")
+        if not hasattr(self, "X"):
+            self.X = torch.zeros_like(self.B)
+            self.AB32 = torch.zeros(self.AB.numel(), dtype=torch.float32, device=self.device)
+            self.R32 = torch.zeros(self.ipiv.numel(), dtype=torch.float32, device=self.device)
+            self.iters = torch.zeros(self.count, dtype=torch.int32, device=self.device)
+            self.berr = torch.zeros(self.count, dtype=torch.float64, device=self.device)
+        st = ctypes.c_void_p(stream) if stream is not None else _stream(self.device)
+        _lib.call("bm_dsgbsv_batched", self.count, _ptr(self.descs), _ptr(self.order), _ptr(self.AB), _ptr(self.B),
+                  _ptr(self.X), _ptr(self.ipiv), _ptr(self.info), _ptr(self.AB32), _ptr(self.R32), _ptr(self.iters),
+                  _ptr(self.berr), _ptr(self.counter), ctypes.c_double(tol), int(maxit), self.max_kl, self.max_ku, st)
+        return self.X
+
+    def solution(self, s: int) -> torch.Tensor:
+        """System s's solution from solve_mixed (n x nrhs view of X)."""
+        n, k, off = int(self.n[s]), int(self.nrhs[s]), int(self.b_off[s])
+        return self.X[off: off + n * k].view(k, n).t()
+
     def capture(self) -> torch.cuda.CUDAGraph:
         """Capture factor_solve in a CUDA graph (call once eagerly first for device set-up)."""
         g = torch.cuda.CUDAGraph()

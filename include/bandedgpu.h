@@ -131,6 +131,23 @@ int bm_dgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *orde
 int bm_sgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, float *AB, int64_t *ipiv,
                      float *B, int64_t *info, int32_t *counter, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
 
+/* Mixed-precision refined batched solve (LAPACK DSGESV's scheme on band storage):
+ * each system's FP64 band (AB, gbtrf storage, matrix in rows kl..; read only) is
+ * rounded to FP32 into AB32 (same offsets) and factored in FP32 with partial
+ * pivoting; every right-hand side B (read only) is solved in FP32 and refined with
+ * FP64 residuals r = b - A x and FP64 updates until the backward error
+ * ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol or maxit corrections.  X
+ * receives the solutions (B's layout), iters/berr the corrections taken and the
+ * final backward error per system (max over its right-hand sides), info the FP32
+ * factorization's info.  R32 is FP32 workspace of n floats per system at the
+ * system's ipiv_offset; counter is one int32 of workspace.  No counterpart in the
+ * reference; per system it replaces lu! + ldiv! (src/banded/BandedLU.jl:90-103,
+ * src/banded/linalg.jl:24-30) when the caller accepts a backward-error target. */
+int bm_dsgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const double *AB,
+                      const double *B, double *X, int64_t *ipiv, int64_t *info, float *AB32, float *R32,
+                      int32_t *iters, double *berr, int32_t *counter, double tol, int64_t maxit, int64_t max_kl,
+                      int64_t max_ku, bm_stream_t stream);
+
 /* Allocation-free variant of bm_dgbsv_batched, for callers that cannot allocate
  * device memory when they solve: code running under CUDA stream capture, real-time
  * loops that must not block on an allocator, and hosts whose device memory belongs
