@@ -91,7 +91,7 @@ class BandedBatch:
         if not hasattr(self, "X"):
             self.X = torch.zeros_like(self.B)
             self.AB32 = torch.zeros(self.AB.numel(), dtype=torch.float32, device=self.device)
-            self.R32 = torch.zeros(self.ipiv.numel(), dtype=torch.float32, device=self.device)
+            self.R32 = torch.zeros(self.B.numel(), dtype=torch.float32, device=self.device)
             self.iters = torch.zeros(self.count, dtype=torch.int32, device=self.device)
             self.berr = torch.zeros(self.count, dtype=torch.float64, device=self.device)
         st = ctypes.c_void_p(stream) if stream is not None else _stream(self.device)

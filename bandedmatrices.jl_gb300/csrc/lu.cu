@@ -11,51 +11,54 @@ namespace bm {
 
 constexpr int kP = 4;  // rows staged ahead by cp.async in gbtrf
 
-template <typename T>
-__global__ void __launch_bounds__(32) gbtrf_one_kernel(i64 m, i64 n, int kl, int ku, T* ab, i64 ldab, i64* ipiv,
-                                                       i64* info) {
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * G) gbtrf_one_kernel(i64 m, i64 n, int kl, int ku, T* ab, i64 ldab, i64* ipiv,
+                                                           i64* info) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const i64 r = gbtrf_warp<T, kP>(m, n, kl, ku, ab, ldab, ipiv, reinterpret_cast<T*>(smem_raw));
+  const i64 r = gbtrf_group<T, kP, G>(m, n, kl, ku, ab, ldab, ipiv, reinterpret_cast<T*>(smem_raw));
   if (threadIdx.x == 0) *info = r;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(32) gbtrs_one_kernel(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* ab,
-                                                       i64 ldab, const i64* ipiv, T* B, i64 ldb) {
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* ab,
+                                                           i64 ldab, const i64* ipiv, T* B, i64 ldb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  for (i64 r = blockIdx.x; r < nrhs; r += gridDim.x)
-    gbtrs_warp<T>(trans, n, kl, ku, ab, ldab, ipiv, B + r * ldb, reinterpret_cast<T*>(smem_raw));
+  // block r sweeps right-hand sides [r*kMaxRhs, (r+1)*kMaxRhs)
+  for (i64 r = blockIdx.x; r * kMaxRhs < nrhs; r += gridDim.x)
+    gbtrs_all<T, G>(trans, n, kl, ku, min((i64)kMaxRhs, nrhs - r * kMaxRhs), ab, ldab, ipiv, B + r * kMaxRhs * ldb,
+                    ldb, reinterpret_cast<T*>(smem_raw));
 }
 
-// Persistent batched factor + solve.  Each warp takes the next system from a
-// device work queue (an atomic counter over `order`, which lists systems from the
-// most to the least expensive), factors it in place and solves its right-hand
-// sides.  Shared memory per warp is sized for the widest band of the batch.
-template <typename T>
-__global__ void __launch_bounds__(128) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
-                                                           const int32_t* __restrict__ order, T* AB, i64* ipiv,
-                                                           T* B, i64* info, int32_t* counter, i64 warp_elems) {
+// Persistent batched factor + solve.  Each group (G = 1: each warp; G > 1: the CTA)
+// takes the next system from a device work queue (an atomic counter over `order`,
+// which lists systems from the most to the least expensive), factors it in place and
+// solves its right-hand sides.  Shared memory per group is sized for the widest band
+// of the batch.
+template <typename T, int G>
+__global__ void __launch_bounds__(G == 1 ? 128 : 32 * G) gbsv_batched_kernel(
+    i64 count, const bm_gb_desc* __restrict__ descs, const int32_t* __restrict__ order, T* AB, i64* ipiv, T* B,
+    i64* info, int32_t* counter, i64 group_elems) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* smem = reinterpret_cast<T*>(smem_raw) + warp * warp_elems;
+  const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
+  T* smem = reinterpret_cast<T*>(smem_raw) + grp * group_elems;
+  int* hdr = reinterpret_cast<int*>(smem);
   for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(counter, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
+    const int idx = next_item<G>(counter, hdr);
     if (idx >= count) break;
     const int s = order ? order[idx] : idx;
     const bm_gb_desc d = descs[s];
     T* ab = AB + d.ab_offset;
     i64* ip = ipiv + d.ipiv_offset;
-    const i64 r = gbtrf_warp<T, kP>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
-    if (lane == 0) info[s] = r;
-    __syncwarp();
-    if (r == 0)
-      for (i64 c = 0; c < d.nrhs; ++c)
-        gbtrs_warp<T>(false, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, B + d.b_offset + c * d.ldb, smem);
-    __syncwarp();
+    const i64 r = gbtrf_group<T, kP, G>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
+    if (Grp<G>::tid() == 0) info[s] = r;
+    Grp<G>::sync();
+    if (r == 0) gbtrs_all<T, G>(false, d.n, (int)d.kl, (int)d.ku, d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem);
+    Grp<G>::sync();
   }
 }
+
+// One group of G warps per system pays off once the window holds a few hundred entries.
+inline bool use_cta_group(i64 kl, i64 ku) { return (kl + 1) * (kl + ku + 1) >= 512; }
 
 template <typename T>
 static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
@@ -74,9 +77,15 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
               (long long)ku);
     return BM_ERR_UNSUPPORTED;
   }
-  int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T>, (int)bytes), name);
-  if (r) return r;
-  gbtrf_one_kernel<T><<<1, 32, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+  if (use_cta_group(kl, ku)) {
+    int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T, 4>, (int)bytes), name);
+    if (r) return r;
+    gbtrf_one_kernel<T, 4><<<1, 128, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+  } else {
+    int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T, 1>, (int)bytes), name);
+    if (r) return r;
+    gbtrf_one_kernel<T, 1><<<1, 32, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+  }
   return launch_status(name);
 }
 
@@ -97,11 +106,18 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
     set_error("%s: band too wide for the staged solve", name);
     return BM_ERR_UNSUPPORTED;
   }
-  int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T>, (int)bytes), name);
-  if (r) return r;
-  const i64 grid = std::min<i64>(nrhs, 65535);
-  gbtrs_one_kernel<T><<<(unsigned)grid, 32, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab, ipiv,
-                                                                   B, ldb);
+  const i64 grid = std::min<i64>(ceil_div(nrhs, kMaxRhs), 65535);
+  if ((kl + ku + 1) * std::min<i64>(nrhs, kMaxRhs) >= 256) {
+    int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T, 4>, (int)bytes), name);
+    if (r) return r;
+    gbtrs_one_kernel<T, 4><<<(unsigned)grid, 128, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab,
+                                                                         ipiv, B, ldb);
+  } else {
+    int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T, 1>, (int)bytes), name);
+    if (r) return r;
+    gbtrs_one_kernel<T, 1><<<(unsigned)grid, 32, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab,
+                                                                        ipiv, B, ldb);
+  }
   return launch_status(name);
 }
 
@@ -122,20 +138,27 @@ static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* 
     set_error("%s: widest band of the batch exceeds the per-warp window limit", name);
     return BM_ERR_UNSUPPORTED;
   }
-  // warps per CTA: as many as fit in ~100 KB (two CTAs per SM), at most 4
-  int wpc = (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
+  const bool cta = use_cta_group(max_kl, max_ku);
+  // G = 1: as many warps per CTA as fit in ~100 KB (at most 4); G = 4: one system per CTA
+  const int wpc = cta ? 1 : (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
+  const int threads = cta ? 128 : 32 * wpc;
   const int smem = (int)(wpc * wbytes);
-  int r = cuda_status(ensure_smem((const void*)gbsv_batched_kernel<T>, smem), name);
+  const void* kfn = cta ? (const void*)gbsv_batched_kernel<T, 4> : (const void*)gbsv_batched_kernel<T, 1>;
+  int r = cuda_status(ensure_smem(kfn, smem), name);
   if (r) return r;
   int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gbsv_batched_kernel<T>, 32 * wpc, smem), name);
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem), name);
   if (r) return r;
   per_sm = std::max(per_sm, 1);
   const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(count, wpc));
   r = cuda_status(cudaMemsetAsync(counter, 0, sizeof(int32_t), stream), name);
   if (r) return r;
-  gbsv_batched_kernel<T><<<(unsigned)grid, 32 * wpc, smem, stream>>>(count, descs, order, AB, ipiv, B, info, counter,
-                                                                     welems_aligned);
+  if (cta)
+    gbsv_batched_kernel<T, 4><<<(unsigned)grid, threads, smem, stream>>>(count, descs, order, AB, ipiv, B, info,
+                                                                          counter, welems_aligned);
+  else
+    gbsv_batched_kernel<T, 1><<<(unsigned)grid, threads, smem, stream>>>(count, descs, order, AB, ipiv, B, info,
+                                                                          counter, welems_aligned);
   return launch_status(name);
 }
 

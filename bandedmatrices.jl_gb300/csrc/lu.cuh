@@ -1,27 +1,73 @@
-// Warp-level banded LU (xGBTF2 semantics) and solves (xGBTRS), shared by the
-// single-system entry points and the batched persistent kernel.
+// Banded LU (xGBTF2 semantics) and solves (xGBTRS) executed by a group of G warps
+// (G = 1: one warp; G > 1: the whole CTA, one warp per SM sub-partition, so a wide
+// band gets the SM's full FP64/FP32 throughput).  Shared by the single-system entry
+// points, the batched persistent kernels and the mixed-precision solve.
 //
-// gbtrf: one warp factors one system.  The active part of the matrix at step j is
-// the (kl+1) x (kl+ku+1) window A(j:j+kl, j:j+kl+ku); it lives in shared memory
-// as a ring in both dimensions (logical row r <-> physical (j+r) mod (kl+1),
-// logical column c <-> (j+c) mod (kl+ku+1)), so the window slides by one row
-// and one column per step without moving data.  The row that enters at each
-// step is fetched P steps ahead with cp.async into a staging ring.  The
-// arithmetic is LAPACK's dgbtf2 operation for operation: idamax (first index of
-// the largest |a|), row interchange over columns j..ju, scaling by the
-// reciprocal of the pivot, and the rank-1 update a <- fma(l_i, -u_c, a) skipping
-// u_c == 0 -- so factors and pivots equal the oracle's bit for bit.
+// gbtrf: the active part of the matrix at step j is the (kl+1) x (kl+ku+1) window
+// A(j:j+kl, j:j+kl+ku); it lives in shared memory as a ring in both dimensions
+// (logical row r <-> physical (j+r) mod (kl+1), logical column c <-> (j+c) mod
+// (kl+ku+1)), so the window slides one row and one column per step without moving
+// data.  The row that enters at each step is fetched P steps ahead with cp.async
+// into a staging ring.  The arithmetic is LAPACK's dgbtf2 operation for operation:
+// idamax (first index of the largest |a|), row interchange over columns j..ju,
+// scaling by the reciprocal of the pivot, and the rank-1 update a <- fma(l_i, -u_c, a)
+// skipping u_c == 0 -- so factors and pivots equal the oracle's bit for bit.
 //
-// gbtrs: one warp sweeps one right-hand side.  The sweeps are sequential in j;
-// each step's update is spread over the lanes and b is staged through shared
-// memory in chunks of kChunk steps.  Every element receives its updates in the
-// same order as in dgbtrs/dtbsv (the transposed triangular solve is done in
-// axpy form, which preserves each element's accumulation order).  Only the
-// L^T dot products of the transposed solve use a tree reduction when kl > 16.
+// gbtrs: the sweeps are sequential in j; each step's update is spread over the
+// group's threads, up to kMaxRhs right-hand sides at once, and b is staged through
+// shared memory in chunks of kChunk steps.  Every element receives its updates in
+// the same order as in dgbtrs/dtbsv (the transposed triangular solve is done in axpy
+// form, which preserves each element's accumulation order).  Only the L^T dot
+// products of the transposed solve use a tree reduction when kl > 16.
 #pragma once
 #include "common.cuh"
 
 namespace bm {
+
+// ------------------------------------------------------------ group helpers
+template <int G>
+struct Grp {
+  static constexpr int NT = 32 * G;
+  // G == 1: several independent warps per CTA; G > 1: one group per CTA
+  static __device__ __forceinline__ int tid() { return G == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+  static __device__ __forceinline__ void sync() {
+    if (G == 1) __syncwarp();
+    else __syncthreads();
+  }
+};
+
+// Next work item for the calling group (an atomic counter), broadcast to the group
+// through hdr (the group's shared-memory header).
+template <int G>
+__device__ __forceinline__ int next_item(int32_t* counter, int* hdr) {
+  int idx = 0;
+  if (Grp<G>::tid() == 0) idx = atomicAdd(counter, 1);
+  if (G == 1) return __shfl_sync(0xffffffffu, idx, 0);
+  if (threadIdx.x == 0) hdr[1] = idx;
+  __syncthreads();
+  idx = hdr[1];
+  __syncthreads();
+  return idx;
+}
+
+// Group-wide maximum (NaN propagates); scratch: G doubles of shared memory.
+template <int G>
+__device__ __forceinline__ double grp_max(double v, double* scratch) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    const double o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = (o > v || o != o) ? o : v;
+  }
+  if (G == 1) return v;
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) scratch[w] = v;
+  __syncthreads();
+  v = scratch[0];
+  for (int k = 1; k < G; ++k) v = (scratch[k] > v || scratch[k] != scratch[k]) ? scratch[k] : v;
+  __syncthreads();
+  return v;
+}
 
 // ------------------------------------------------------------ cp.async helpers
 template <typename T>
@@ -39,72 +85,78 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Shared-memory footprint (elements of T) of one warp's gbtrf window + staging ring.
+// Shared-memory footprints, in elements of T.  Every group region starts with a
+// kHdr-element header (scalars broadcast between the group's warps).
+constexpr int kHdr = 16;
 __host__ __device__ inline int lu_rs(int kl) { return (kl + 1) | 1; }  // odd column stride: no bank conflicts
 template <int P>
 __host__ __device__ inline i64 gbtrf_smem_elems(int kl, int ku) {
   const int K = kl + ku + 1;
-  return (i64)lu_rs(kl) * K + (i64)P * K;
+  return kHdr + (i64)lu_rs(kl) * K + (i64)P * K;
 }
 
 constexpr int kChunk = 32;  // solve steps staged per chunk
+constexpr int kMaxRhs = 8;  // right-hand sides swept together
 __host__ __device__ inline i64 gbtrs_smem_elems(int kl, int ku) {
   const int kv = kl + ku;
-  // ipiv chunk (kChunk int64, as 2*kChunk T slots) + window of b (kChunk + kv + 1)
-  // + chunk of L or U columns (kChunk x (kv+1))
-  return 2 * kChunk + (i64)(kChunk + kv + 1) + (i64)kChunk * (kv + 1);
+  // header + ipiv chunk (kChunk int64, as 2*kChunk T slots) + window of b
+  // ((kChunk+kv+1) rows x kMaxRhs) + chunk of L or U columns (kChunk x (kv+1))
+  return kHdr + 2 * kChunk + (i64)(kChunk + kv + 1) * kMaxRhs + (i64)kChunk * (kv + 1);
 }
 
-// X[s] <- X[s + d] for s in [0, count), d >= 0 (warp-cooperative, overlap-safe)
-template <typename T>
-__device__ __forceinline__ void warp_shift_down(T* X, int count, int d) {
-  const int lane = threadIdx.x & 31;
-  for (int s0 = 0; s0 < count; s0 += 32) {
-    const int s = s0 + lane;
+// X[s] <- X[s + d] for s in [0, count), d >= 0 (group-cooperative, overlap-safe)
+template <typename T, int G>
+__device__ __forceinline__ void grp_shift_down(T* X, int count, int d) {
+  const int t = Grp<G>::tid();
+  for (int s0 = 0; s0 < count; s0 += Grp<G>::NT) {
+    const int s = s0 + t;
     const T v = (s < count) ? X[s + d] : T(0);
-    __syncwarp();
+    Grp<G>::sync();
     if (s < count) X[s] = v;
-    __syncwarp();
+    Grp<G>::sync();
   }
 }
-// X[s] <- X[s - d] for s in [d, d + count), d >= 0, processed from the top
-template <typename T>
-__device__ __forceinline__ void warp_shift_up(T* X, int count, int d) {
-  const int lane = threadIdx.x & 31;
-  for (int s0 = count - 1; s0 >= 0; s0 -= 32) {
-    const int s = s0 - lane;  // relative index, descending
+// X[s + d] <- X[s] for s in [0, count), d >= 0, processed from the top
+template <typename T, int G>
+__device__ __forceinline__ void grp_shift_up(T* X, int count, int d) {
+  const int t = Grp<G>::tid();
+  for (int s0 = count - 1; s0 >= 0; s0 -= Grp<G>::NT) {
+    const int s = s0 - t;
     const T v = (s >= 0) ? X[s] : T(0);
-    __syncwarp();
+    Grp<G>::sync();
     if (s >= 0) X[s + d] = v;
-    __syncwarp();
+    Grp<G>::sync();
   }
 }
 
 // --------------------------------------------------------------------- gbtrf
 // Factors the m x n band in ab (LAPACK gbtrf storage, ldab >= 2kl+ku+1) in place;
-// writes 1-based pivots to ipiv[0..min(m,n)) and returns LAPACK's info.
-template <typename T, int P>
-__device__ i64 gbtrf_warp(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab, i64* __restrict__ ipiv,
-                          T* __restrict__ smem) {
-  const int lane = threadIdx.x & 31;
+// writes 1-based pivots to ipiv[0..min(m,n)) and returns LAPACK's info (to every
+// thread of the group).
+template <typename T, int P, int G>
+__device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab, i64* __restrict__ ipiv,
+                           T* __restrict__ smem) {
+  constexpr int NT = Grp<G>::NT;
+  const int tid = Grp<G>::tid(), lane = threadIdx.x & 31, wig = tid >> 5;
   const int kv = kl + ku, R = kl + 1, K = kv + 1, RS = lu_rs(kl);
-  T* W = smem;
-  T* S = smem + (i64)RS * K;
+  int* hdr = reinterpret_cast<int*>(smem);
+  T* W = smem + kHdr;
+  T* S = W + (i64)RS * K;
   const i64 mn = min(m, n);
   i64 info = 0;
   if (mn <= 0) return 0;
 
   // initial window: matrix rows 0..kl, columns 0..kv
-  for (int e = lane; e < R * K; e += 32) {
+  for (int e = tid; e < R * K; e += NT) {
     const int c = e / R, r = e - c * R;
     T v = T(0);
     if (r < m && c < n && r - c <= kl && c - r <= ku) v = ab[(kv + r - c) + (i64)c * ldab];
     W[r + c * RS] = v;
   }
-  // rows kl+1 .. kl+P into the staging ring (one cp.async group per row)
+  // rows kl+1 .. kl+P into the staging ring (one cp.async group per row and thread)
   auto issue_row = [&](i64 i) {
     T* dst = S + (int)(i & (P - 1)) * K;
-    for (int c = lane; c < K; c += 32) {
+    for (int c = tid; c < K; c += NT) {
       const i64 col = i - kl + c;
       const bool ok = i < m && col < n;
       cp_async_elem(dst + c, ok ? ab + (kv + kl - c) + col * ldab : ab, ok);
@@ -112,35 +164,45 @@ __device__ i64 gbtrf_warp(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 
     cp_async_commit();
   };
   for (int p = 0; p < P; ++p) issue_row((i64)kl + 1 + p);
-  __syncwarp();
+  Grp<G>::sync();
 
   int pr0 = 0, pc0 = 0;
   i64 ju = 0;
   for (i64 j = 0; j < mn; ++j) {
     const int km = (int)min((i64)kl, m - 1 - j);
-    // ---- pivot: first index of max |a| over logical rows 0..km of logical column 0
-    T best = T(-1);
-    int bidx = 0x7fffffff;
-    for (int r = lane; r <= km; r += 32) {
-      int pr = pr0 + r;
-      pr = pr >= R ? pr - R : pr;
-      const T v = fabs(W[pr + pc0 * RS]);
-      if (bidx == 0x7fffffff || v > best) {
-        best = v;
-        bidx = r;
+    // ---- pivot (warp 0): first index of max |a| over logical rows 0..km of column 0
+    int jp = 0;
+    if (wig == 0) {
+      T best = T(-1);
+      int bidx = 0x7fffffff;
+      for (int r = lane; r <= km; r += 32) {
+        int pr = pr0 + r;
+        pr = pr >= R ? pr - R : pr;
+        const T v = fabs(W[pr + pc0 * RS]);
+        if (bidx == 0x7fffffff || v > best) {
+          best = v;
+          bidx = r;
+        }
       }
-    }
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-      const T ov = __shfl_down_sync(0xffffffffu, best, off);
-      const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
-      if (lane + off < 32 && (ov > best || (ov == best && oi < bidx))) {
-        best = ov;
-        bidx = oi;
+      for (int off = 16; off >= 1; off >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
+        if (lane + off < 32 && (ov > best || (ov == best && oi < bidx))) {
+          best = ov;
+          bidx = oi;
+        }
+      }
+      jp = __shfl_sync(0xffffffffu, bidx, 0);
+      if (lane == 0) {
+        ipiv[j] = j + jp + 1;
+        if (G > 1) hdr[0] = jp;
       }
     }
-    const int jp = __shfl_sync(0xffffffffu, bidx, 0);
-    if (lane == 0) ipiv[j] = j + jp + 1;
+    if (G > 1) {
+      Grp<G>::sync();
+      jp = hdr[0];
+    }
     int prp = pr0 + jp;
     prp = prp >= R ? prp - R : prp;
     const T piv = W[prp + pc0 * RS];
@@ -148,225 +210,281 @@ __device__ i64 gbtrf_warp(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 
       ju = max(ju, min(j + ku + jp, n - 1));
       const int nc = (int)(ju - j);
       if (jp != 0) {
-        for (int c = lane; c <= nc; c += 32) {
+        for (int c = tid; c <= nc; c += NT) {
           int pc = pc0 + c;
           pc = pc >= K ? pc - K : pc;
           const T t = W[pr0 + pc * RS];
           W[pr0 + pc * RS] = W[prp + pc * RS];
           W[prp + pc * RS] = t;
         }
-        __syncwarp();
+        Grp<G>::sync();
       }
       if (km > 0) {
         const T rcp = T(1) / piv;
-        for (int r = 1 + lane; r <= km; r += 32) {
+        for (int r = 1 + tid; r <= km; r += NT) {
           int pr = pr0 + r;
           pr = pr >= R ? pr - R : pr;
           W[pr + pc0 * RS] = rcp * W[pr + pc0 * RS];
         }
-        __syncwarp();
-        for (int c = 1 + lane; c <= nc; c += 32) {
+        Grp<G>::sync();
+        // rank-1 update: threads own columns; rows go in chunks of kU so that a chunk's
+        // shared-memory loads are all in flight before its stores
+        constexpr int kU = 8;
+        const T* col0 = W + pc0 * RS;
+        for (int c = 1 + tid; c <= nc; c += NT) {
           int pc = pc0 + c;
           pc = pc >= K ? pc - K : pc;
-          const T uc = W[pr0 + pc * RS];
+          T* colc = W + pc * RS;
+          const T uc = colc[pr0];
           if (uc != T(0)) {
             const T t = -uc;
             int pr = pr0;
-            for (int r = 1; r <= km; ++r) {
-              pr = pr + 1 == R ? 0 : pr + 1;
-              W[pr + pc * RS] = fma(W[pr + pc0 * RS], t, W[pr + pc * RS]);
+            for (int r0 = 1; r0 <= km; r0 += kU) {
+              T mv[kU], av[kU];
+              int pq[kU];
+#pragma unroll
+              for (int q = 0; q < kU; ++q) {
+                pr = pr + 1 == R ? 0 : pr + 1;
+                pq[q] = pr;
+                if (r0 + q <= km) {
+                  mv[q] = col0[pr];
+                  av[q] = colc[pr];
+                }
+              }
+#pragma unroll
+              for (int q = 0; q < kU; ++q)
+                if (r0 + q <= km) colc[pq[q]] = fma(mv[q], t, av[q]);
             }
           }
         }
-        __syncwarp();
+        Grp<G>::sync();
       }
     } else if (info == 0) {
       info = j + 1;
     }
     // ---- U row j (logical row 0) and L column j are final
     const int ncw = (int)min((i64)kv, n - 1 - j);
-    for (int c = lane; c <= ncw; c += 32) {
+    for (int c = tid; c <= ncw; c += NT) {
       int pc = pc0 + c;
       pc = pc >= K ? pc - K : pc;
       ab[(kv - c) + (j + c) * ldab] = W[pr0 + pc * RS];
     }
-    for (int r = 1 + lane; r <= km; r += 32) {
+    for (int r = 1 + tid; r <= km; r += NT) {
       int pr = pr0 + r;
       pr = pr >= R ? pr - R : pr;
       ab[(kv + r) + j * ldab] = W[pr + pc0 * RS];
     }
-    __syncwarp();
+    Grp<G>::sync();
     if (j + 1 == mn) break;
     // ---- slide: row j+1+kl enters physical row pr0, column j+1+kv enters physical column pc0
-    for (int r = lane; r < R; r += 32) W[r + pc0 * RS] = T(0);
+    for (int r = tid; r < R; r += NT) W[r + pc0 * RS] = T(0);
     cp_async_wait<P - 1>();
-    __syncwarp();
+    Grp<G>::sync();
     const i64 inew = j + 1 + kl;
     const T* st = S + (int)(inew & (P - 1)) * K;
-    for (int c = lane; c < K; c += 32) {
+    for (int c = tid; c < K; c += NT) {
       int pc = pc0 + 1 + c;
       pc = pc >= K ? pc - K : pc;
       W[pr0 + pc * RS] = st[c];
     }
-    __syncwarp();
+    Grp<G>::sync();
     issue_row(inew + P);
     pr0 = pr0 + 1 == R ? 0 : pr0 + 1;
     pc0 = pc0 + 1 == K ? 0 : pc0 + 1;
   }
   cp_async_wait<0>();
-  __syncwarp();
+  Grp<G>::sync();
   return info;
 }
 
 // --------------------------------------------------------------------- gbtrs
-// Solves op(A) x = b for one right-hand side b (length n, contiguous) with the
-// gbtrf factors.  trans: false = 'N', true = 'T'.
-template <typename T>
-__device__ void gbtrs_warp(bool trans, i64 n, int kl, int ku, const T* __restrict__ ab, i64 ldab,
-                           const i64* __restrict__ ipiv, T* __restrict__ b, T* __restrict__ smem) {
-  const int lane = threadIdx.x & 31;
+// Thread layout for a group of nr <= kMaxRhs right-hand sides: nr is padded to a
+// power of two 1 << lg; thread -> (row offset tid >> lg, column tid & ((1<<lg)-1)),
+// rows advancing by NT >> lg.  Window element (row s, column c) lives at X[s*nr + c].
+__device__ __forceinline__ int rhs_lg(int nr) { return nr <= 1 ? 0 : nr <= 2 ? 1 : nr <= 4 ? 2 : 3; }
+
+// Solves op(A) X = B for nr <= kMaxRhs right-hand sides (B: n x nr, leading dim ldb)
+// with the gbtrf factors; trans: false = 'N', true = 'T'.
+template <typename T, int G>
+__device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* __restrict__ ab, i64 ldab,
+                            const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem) {
+  constexpr int NT = Grp<G>::NT;
+  const int tid = Grp<G>::tid(), lane = threadIdx.x & 31, wig = tid >> 5;
   const int kv = kl + ku;
-  if (n <= 0) return;
-  i64* IP = reinterpret_cast<i64*>(smem);     // kChunk pivots (8-byte aligned: smem is)
-  T* X = smem + 2 * kChunk;                   // window of b: XW entries
+  const int lg = rhs_lg(nr), cl = tid & ((1 << lg) - 1), rstep = NT >> lg, r0 = tid >> lg;
+  const bool cok = cl < nr;
+  i64* IP = reinterpret_cast<i64*>(smem + kHdr);  // kChunk pivots (8-byte aligned)
+  T* X = smem + kHdr + 2 * kChunk;                // window: XW rows x nr
   const int XW = kChunk + kv + 1;
-  T* LC = X + XW;                             // kChunk columns x (kv+1)
+  T* LC = X + XW * kMaxRhs;                       // kChunk columns x (kv+1)
+  auto sync = [] { Grp<G>::sync(); };
+  // copy window rows [s0, s1) from/to b rows [g0 + s0, ...), zero outside [0, n)
+  auto load_rows = [&](int s0, int s1, i64 g0) {
+    for (int sr = s0 + r0; sr < s1; sr += rstep)
+      if (cok) X[sr * nr + cl] = (g0 + sr >= 0 && g0 + sr < n) ? b[(g0 + sr) + cl * ldb] : T(0);
+  };
+  auto store_rows = [&](int s0, int s1, i64 g0) {
+    for (int sr = s0 + r0; sr < s1; sr += rstep)
+      if (cok && g0 + sr >= 0 && g0 + sr < n) b[(g0 + sr) + cl * ldb] = X[sr * nr + cl];
+  };
 
   if (!trans) {
     // ---- forward: L with row interchanges (dgbtrs 'N': dswap + dger per column)
     if (kl > 0 && n > 1) {
-      // X[s] = b[j0 + s]; kl entries are carried from one chunk to the next
-      for (int s = lane; s < kl; s += 32) X[s] = (s < n) ? b[s] : T(0);
+      load_rows(0, kl, 0);
       for (i64 j0 = 0; j0 < n - 1; j0 += kChunk) {
         const int jn = (int)min((i64)kChunk, n - 1 - j0);
-        for (int s = kl + lane; s < jn + kl; s += 32) X[s] = (j0 + s < n) ? b[j0 + s] : T(0);
-        for (int e = lane; e < jn * kl; e += 32) {
-          const int s = e / kl, i = e - s * kl;
-          LC[s * kl + i] = (j0 + s + 1 + i < n) ? ab[(kv + 1 + i) + (j0 + s) * ldab] : T(0);
+        load_rows(kl, jn + kl, j0);
+        for (int e = tid; e < jn * kl; e += NT) {
+          const int sidx = e / kl, i = e - sidx * kl;
+          LC[sidx * kl + i] = (j0 + sidx + 1 + i < n) ? ab[(kv + 1 + i) + (j0 + sidx) * ldab] : T(0);
         }
-        for (int s = lane; s < jn; s += 32) IP[s] = ipiv[j0 + s] - 1 - j0;
-        __syncwarp();
-        for (int s = 0; s < jn; ++s) {
-          const int lm = (int)min((i64)kl, n - 1 - (j0 + s));
-          const int l = (int)IP[s];
-          if (l != s && lane == 0) {
-            const T t = X[l];
-            X[l] = X[s];
-            X[s] = t;
+        for (int sidx = tid; sidx < jn; sidx += NT) IP[sidx] = ipiv[j0 + sidx] - 1 - j0;
+        sync();
+        for (int st = 0; st < jn; ++st) {
+          const int lm = (int)min((i64)kl, n - 1 - (j0 + st));
+          const int l = (int)IP[st];
+          if (l != st) {
+            if (tid < nr) {
+              const T t = X[l * nr + tid];
+              X[l * nr + tid] = X[st * nr + tid];
+              X[st * nr + tid] = t;
+            }
+            sync();
           }
-          __syncwarp();
-          const T bj = X[s];
-          if (bj != T(0)) {
-            const T t = -bj;
-            for (int i = lane; i < lm; i += 32) X[s + 1 + i] = fma(LC[s * kl + i], t, X[s + 1 + i]);
+          if (cok) {
+            const T bj = X[st * nr + cl];
+            if (bj != T(0)) {
+              const T t = -bj;
+              for (int i = r0; i < lm; i += rstep)
+                X[(st + 1 + i) * nr + cl] = fma(LC[st * kl + i], t, X[(st + 1 + i) * nr + cl]);
+            }
           }
-          __syncwarp();
+          sync();
         }
-        for (int s = lane; s < jn; s += 32) b[j0 + s] = X[s];
-        __syncwarp();
-        warp_shift_down(X, kl, jn);  // carry X[jn .. jn+kl) to the front
-        if (j0 + jn >= n - 1)
-          for (int s = lane; s < kl; s += 32)
-            if (j0 + jn + s < n) b[j0 + jn + s] = X[s];
-        __syncwarp();
+        store_rows(0, jn, j0);
+        sync();
+        grp_shift_down<T, G>(X, kl * nr, jn * nr);  // carry rows jn .. jn+kl to the front
+        if (j0 + jn >= n - 1) store_rows(0, kl, j0 + jn);
+        sync();
       }
     }
-    // ---- backward: U x = y (dtbsv 'U','N','N', bandwidth kv), columns n-1 .. 0
-    // X[s] = b[base + s] with X[XW-1] = b[j1] at the start of each chunk
+    // ---- backward: U x = y (dtbsv 'U','N','N', bandwidth kv), columns n-1 .. 0;
+    // window row s <-> b row base + s, with row XW-1 = j1 at the start of each chunk
     i64 j1 = n - 1;
     i64 base = j1 - (XW - 1);
-    for (int s = lane; s < XW; s += 32) X[s] = (base + s >= 0) ? b[base + s] : T(0);
-    __syncwarp();
+    load_rows(0, XW, base);
+    sync();
     while (true) {
       const int jn = (int)min((i64)kChunk, j1 + 1);
       // U(j-i, j) = ab[(kv-i) + j*ldab], i = 0..kv, for j = j1, j1-1, ...
-      for (int e = lane; e < jn * (kv + 1); e += 32) {
+      for (int e = tid; e < jn * (kv + 1); e += NT) {
         const int t = e / (kv + 1), i = e - t * (kv + 1);
         const i64 j = j1 - t;
         LC[e] = (j - i >= 0) ? ab[(kv - i) + j * ldab] : T(0);
       }
-      __syncwarp();
+      sync();
       for (int t = 0; t < jn; ++t) {
         const i64 j = j1 - t;
         const int xs = (int)(j - base);
-        const T xj = X[xs];
-        if (xj != T(0)) {
-          const T v = xj / LC[t * (kv + 1)];
-          __syncwarp();
-          if (lane == 0) X[xs] = v;
-          const T tt = -v;
-          const int lim = (int)min((i64)kv, j);
-          for (int i = 1 + lane; i <= lim; i += 32) X[xs - i] = fma(tt, LC[t * (kv + 1) + i], X[xs - i]);
+        if (tid < nr) {
+          const T xv = X[xs * nr + tid];
+          if (xv != T(0)) X[xs * nr + tid] = xv / LC[t * (kv + 1)];
         }
-        __syncwarp();
+        sync();
+        if (cok) {
+          const T xj = X[xs * nr + cl];
+          if (xj != T(0)) {
+            const T tt = -xj;
+            const int lim = (int)min((i64)kv, j);
+            for (int i = 1 + r0; i <= lim; i += rstep)
+              X[(xs - i) * nr + cl] = fma(tt, LC[t * (kv + 1) + i], X[(xs - i) * nr + cl]);
+          }
+        }
+        sync();
       }
-      for (int t = lane; t < jn; t += 32) b[j1 - t] = X[(int)(j1 - t - base)];
-      __syncwarp();
+      store_rows((int)(j1 - jn + 1 - base), (int)(j1 + 1 - base), base);
+      sync();
       j1 -= jn;
       if (j1 < 0) break;
-      // window moves down by jn: X'[s] = X[s - jn] for s >= jn, X'[s] = b[base' + s] below
-      warp_shift_up(X, XW - jn, jn);
+      grp_shift_up<T, G>(X, (XW - jn) * nr, jn * nr);
       base -= jn;
-      for (int s = lane; s < jn; s += 32) X[s] = (base + s >= 0) ? b[base + s] : T(0);
-      __syncwarp();
+      load_rows(0, jn, base);
+      sync();
     }
   } else {
     // ---- U^T y = b (dtbsv 'U','T','N') in axpy form: once x_i is final, x_c -= U(i,c) x_i
-    for (int s = lane; s < XW; s += 32) X[s] = (s < n) ? b[s] : T(0);
-    __syncwarp();
+    load_rows(0, XW, 0);
+    sync();
     for (i64 j0 = 0; j0 < n; j0 += kChunk) {
       const int jn = (int)min((i64)kChunk, n - j0);
       // row i of U: U(i, i+c) = ab[(kv-c) + (i+c)*ldab], c = 0..kv
-      for (int e = lane; e < jn * (kv + 1); e += 32) {
+      for (int e = tid; e < jn * (kv + 1); e += NT) {
         const int t = e / (kv + 1), c = e - t * (kv + 1);
         const i64 i = j0 + t;
         LC[e] = (i + c < n) ? ab[(kv - c) + (i + c) * ldab] : T(0);
       }
-      __syncwarp();
+      sync();
       for (int t = 0; t < jn; ++t) {
         const i64 i = j0 + t;
-        const T xi = X[t] / LC[t * (kv + 1)];
-        __syncwarp();
-        if (lane == 0) X[t] = xi;
-        const int lim = (int)min((i64)kv, n - 1 - i);
-        for (int c = 1 + lane; c <= lim; c += 32) X[t + c] = fma(-LC[t * (kv + 1) + c], xi, X[t + c]);
-        __syncwarp();
+        if (tid < nr) X[t * nr + tid] = X[t * nr + tid] / LC[t * (kv + 1)];
+        sync();
+        if (cok) {
+          const T xi = X[t * nr + cl];
+          const int lim = (int)min((i64)kv, n - 1 - i);
+          for (int c = 1 + r0; c <= lim; c += rstep)
+            X[(t + c) * nr + cl] = fma(-LC[t * (kv + 1) + c], xi, X[(t + c) * nr + cl]);
+        }
+        sync();
       }
-      for (int t = lane; t < jn; t += 32) b[j0 + t] = X[t];
-      __syncwarp();
-      // window moves up by jn
-      warp_shift_down(X, XW - jn, jn);
-      for (int s = XW - jn + lane; s < XW; s += 32) X[s] = (j0 + jn + s < n) ? b[j0 + jn + s] : T(0);
-      __syncwarp();
+      store_rows(0, jn, j0);
+      sync();
+      grp_shift_down<T, G>(X, (XW - jn) * nr, jn * nr);
+      load_rows(XW - jn, XW, j0 + jn);
+      sync();
     }
     // ---- L^T with interchanges, j = n-2 .. 0 (dgbtrs 'T': dgemv then dswap)
     if (kl > 0) {
       for (i64 j = n - 2; j >= 0; --j) {
         const int lm = (int)min((i64)kl, n - 1 - j);
         const T* lc = ab + (kv + 1) + j * ldab;
-        T temp = T(0);
         if (kl <= 16) {
-          if (lane == 0)
-            for (int i = 0; i < lm; ++i) temp = fma(b[j + 1 + i], lc[i], temp);
-        } else {
-          for (int i = lane; i < lm; i += 32) temp = fma(b[j + 1 + i], lc[i], temp);
+          if (tid < nr) {
+            T temp = T(0);
+            for (int i = 0; i < lm; ++i) temp = fma(b[(j + 1 + i) + tid * ldb], lc[i], temp);
+            b[j + tid * ldb] = fma(T(-1), temp, b[j + tid * ldb]);
+          }
+        } else if (wig == 0) {
+          for (int c = 0; c < nr; ++c) {
+            T temp = T(0);
+            for (int i = lane; i < lm; i += 32) temp = fma(b[(j + 1 + i) + c * ldb], lc[i], temp);
 #pragma unroll
-          for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
-        }
-        if (lane == 0) {
-          b[j] = fma(T(-1), temp, b[j]);
-          const i64 l = ipiv[j] - 1;
-          if (l != j) {
-            const T t = b[l];
-            b[l] = b[j];
-            b[j] = t;
+            for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
+            if (lane == 0) b[j + c * ldb] = fma(T(-1), temp, b[j + c * ldb]);
           }
         }
         __threadfence_block();
-        __syncwarp();
+        sync();
+        const i64 l = ipiv[j] - 1;
+        if (l != j && tid < nr) {
+          const T t = b[l + tid * ldb];
+          b[l + tid * ldb] = b[j + tid * ldb];
+          b[j + tid * ldb] = t;
+        }
+        __threadfence_block();
+        sync();
       }
     }
   }
+}
+
+// All nrhs right-hand sides, kMaxRhs per sweep.
+template <typename T, int G>
+__device__ void gbtrs_all(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* __restrict__ ab, i64 ldab,
+                          const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem) {
+  if (n <= 0) return;
+  for (i64 c0 = 0; c0 < nrhs; c0 += kMaxRhs)
+    gbtrs_group<T, G>(trans, n, kl, ku, (int)min((i64)kMaxRhs, nrhs - c0), ab, ldab, ipiv, b + c0 * ldb, ldb, smem);
 }
 
 }  // namespace bm

@@ -17,66 +17,91 @@
 
 namespace bm {
 
-// r = b - A x for one system, written to r32 (FP32); returns ||r||_inf (FP64).
-// Column-oriented: for each column j, lanes update y[j-ku .. j+kl] (a coalesced read
-// of band column j); a sliding window of y in shared memory holds the partial sums.
-// Rows are emitted once every column that touches them has been added.
-__device__ double residual_warp(i64 n, int kl, int ku, const double* __restrict__ ab, i64 ldab,
-                                const double* __restrict__ b, const double* __restrict__ x, float* __restrict__ r32,
-                                double* __restrict__ Y, double& xnorm) {
+// R = B - A X on rows [rb, re) for up to kResRhs right-hand sides of one system,
+// written to R32 (FP32, leading dim n); returns this warp's partial maxima of |r_c|,
+// |x_c| (over the columns it read) and, with want_anorm, of the |A| row sums.  Each
+// lane owns window rows w = lane + 32q (q < kResQ) in registers; band columns are
+// streamed once per 32-column chunk, every lane reading the entry of its own row (a
+// coalesced read of the column), so no shared memory and no synchronisation are
+// needed.  Row i accumulates its terms in ascending column order.
+constexpr int kResRhs = 4;
+constexpr int kResQ = 5;  // window rows 32*kResQ >= 32 + kl + ku  (kl + ku <= 128)
+
+__device__ void residual_rows(i64 n, i64 rb, i64 re, int kl, int ku, int nr, const double* __restrict__ band,
+                              i64 ldab, const double* __restrict__ B, const double* __restrict__ X, i64 ld,
+                              float* __restrict__ R32, bool want_anorm, double& anorm, double* rnorm,
+                              double* xnorm) {
   const int lane = threadIdx.x & 31;
-  const int kv = kl + ku;          // ab points at the band: A(i,j) = ab[(ku + i - j) + j*ldab]
-  const int W = 32 + kl + ku;      // window: rows j0-ku .. j0+31+kl
-  double rnorm = 0.0, xn = 0.0;
-  for (int s = lane; s < W; s += 32) Y[s] = 0.0;
-  __syncwarp();
-  for (i64 j0 = 0; j0 < n; j0 += 32) {
-    const int jn = (int)min((i64)32, n - j0);
-    // window row index w <-> matrix row j0 - ku + w
+  const int kv = kl + ku;  // band: A(i,j) = band[(ku + i - j) + j*ldab]
+  double Y[kResQ][kResRhs], S[kResQ];
+#pragma unroll
+  for (int q = 0; q < kResQ; ++q) {
+    S[q] = 0.0;
+#pragma unroll
+    for (int c = 0; c < kResRhs; ++c) Y[q][c] = 0.0;
+  }
+  double rn[kResRhs], xn[kResRhs], an = 0.0;
+#pragma unroll
+  for (int c = 0; c < kResRhs; ++c) rn[c] = xn[c] = 0.0;
+
+  auto emit = [&](int q, i64 i) {
+    if (i < rb || i >= re) return;
+#pragma unroll
+    for (int c = 0; c < kResRhs; ++c)
+      if (c < nr) {
+        const double ri = B[i + c * ld] - Y[q][c];
+        R32[i + c * n] = (float)ri;
+        rn[c] = fmax(rn[c], fabs(ri));
+      }
+    an = fmax(an, S[q]);
+  };
+
+  const i64 cb = max((i64)0, rb - kl), ce = min(n, re + ku);
+  for (i64 j0 = cb; j0 < ce; j0 += 32) {
+    const int jn = (int)min((i64)32, ce - j0);
+    // window row w <-> matrix row j0 - ku + w;  column j0 + t touches w = t .. t + kv
     for (int t = 0; t < jn; ++t) {
       const i64 j = j0 + t;
-      const double xj = x[j];
-      if (lane == 0) xn = fmax(xn, fabs(xj));
-      const double* col = ab + j * ldab;  // band column j: matrix rows j-ku .. j+kl
-      for (int r = lane; r <= kv; r += 32) {
-        const i64 i = j - ku + r;
-        if (i >= 0 && i < n) Y[t + r] = fma(col[r], xj, Y[t + r]);
-      }
-      __syncwarp();
-    }
-    // rows j0-ku .. j0-ku+jn-1 (window 0..jn-1) are complete when j0+jn == n or
-    // all their columns (<= i+ku) were seen: i + ku <= j0 + jn - 1  <=>  w <= jn - 1
-    for (int w = lane; w < jn; w += 32) {
-      const i64 i = j0 - ku + w;
-      if (i >= 0 && i < n) {
-        const double ri = b[i] - Y[w];
-        r32[i] = (float)ri;
-        rnorm = fmax(rnorm, fabs(ri));
-      }
-    }
-    __syncwarp();
-    // slide the window by jn
-    warp_shift_down(Y, W - jn, jn);
-    for (int s = W - jn + lane; s < W; s += 32) Y[s] = 0.0;
-    __syncwarp();
-  }
-  // tail rows n-ku .. n-1 (window 0..ku-1 after the last slide)
-  for (int w = lane; w < ku; w += 32) {
-    const i64 i = n - ku + w;
-    if (i >= 0) {
-      const double ri = b[i] - Y[w];
-      r32[i] = (float)ri;
-      rnorm = fmax(rnorm, fabs(ri));
-    }
-  }
+      const double* col = band + j * ldab;
+      double xj[kResRhs];
 #pragma unroll
-  for (int off = 16; off >= 1; off >>= 1) {
-    rnorm = fmax(rnorm, __shfl_xor_sync(0xffffffffu, rnorm, off));
-    xn = fmax(xn, __shfl_xor_sync(0xffffffffu, xn, off));
+      for (int c = 0; c < kResRhs; ++c) {
+        xj[c] = c < nr ? X[j + c * ld] : 0.0;
+        xn[c] = fmax(xn[c], fabs(xj[c]));
+      }
+#pragma unroll
+      for (int q = 0; q < kResQ; ++q) {
+        const int r = lane + 32 * q - t;  // band row for this lane's window row
+        const i64 i = j0 - ku + lane + 32 * q;
+        if (r >= 0 && r <= kv && i >= 0 && i < n) {
+          const double a = col[r];
+#pragma unroll
+          for (int c = 0; c < kResRhs; ++c) Y[q][c] = fma(a, xj[c], Y[q][c]);
+          if (want_anorm) S[q] += fabs(a);
+        }
+      }
+    }
+    if (j0 + 32 < ce) {
+      emit(0, j0 - ku + lane);  // rows j0-ku .. j0-ku+31 are complete
+#pragma unroll
+      for (int q = 0; q < kResQ - 1; ++q) {
+        S[q] = S[q + 1];
+#pragma unroll
+        for (int c = 0; c < kResRhs; ++c) Y[q][c] = Y[q + 1][c];
+      }
+      S[kResQ - 1] = 0.0;
+#pragma unroll
+      for (int c = 0; c < kResRhs; ++c) Y[kResQ - 1][c] = 0.0;
+    } else {
+#pragma unroll
+      for (int q = 0; q < kResQ; ++q) emit(q, j0 - ku + lane + 32 * q);
+    }
   }
-  xnorm = xn;
-  __syncwarp();
-  return rnorm;
+  for (int c = 0; c < kResRhs; ++c) {
+    rnorm[c] = rn[c];
+    xnorm[c] = xn[c];
+  }
+  anorm = an;
 }
 
 struct MixedParams {
@@ -89,98 +114,120 @@ struct MixedParams {
   i64* ipiv;
   i64* info;
   float* AB32;       // FP32 factor storage (same offsets as AB)
-  float* R32;        // FP32 work vector per system (offsets = ipiv offsets)
+  float* R32;        // FP32 work copy of B's layout (leading dim n per system)
   int32_t* iters;    // per system: corrections taken (max over right-hand sides)
   double* berr;      // per system: final backward error (max over right-hand sides)
   int32_t* counter;
   double tol;
   int maxit;
-  i64 warp_elems;    // bytes of shared memory per warp / 4
+  i64 group_elems;   // shared-memory floats per group
 };
 
-__global__ void __launch_bounds__(128) dsgbsv_batched_kernel(const MixedParams p) {
+template <int G>
+__global__ void __launch_bounds__(G == 1 ? 128 : 32 * G) dsgbsv_batched_kernel(const MixedParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float* smem = reinterpret_cast<float*>(smem_raw) + warp * p.warp_elems;
+  constexpr int NT = Grp<G>::NT;
+  const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
+  const int tid = Grp<G>::tid(), wig = tid >> 5;
+  float* smem = reinterpret_cast<float*>(smem_raw) + grp * p.group_elems;
+  int* hdr = reinterpret_cast<int*>(smem);
+  double* red = reinterpret_cast<double*>(smem + kHdr);  // reduction scratch (between phases)
+  auto sync = [] { Grp<G>::sync(); };
   for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(p.counter, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
+    const int idx = next_item<G>(p.counter, hdr);
     if (idx >= p.count) break;
     const int s = p.order ? p.order[idx] : idx;
     const bm_gb_desc d = p.descs[s];
-    const int kl = (int)d.kl, ku = (int)d.ku, kv = kl + ku;
+    const int kl = (int)d.kl, ku = (int)d.ku;
     const i64 n = d.n, ldab = d.ldab;
     const double* A = p.AB + d.ab_offset;
     float* A32 = p.AB32 + d.ab_offset;
     i64* ip = p.ipiv + d.ipiv_offset;
-    float* r32 = p.R32 + d.ipiv_offset;
-    // ---- round to FP32 (top kl rows zero) and ||A||_inf (max row sum of |a_ij|)
-    double anorm = 0.0;
-    for (i64 i0 = 0; i0 < n; i0 += 32) {
-      const i64 i = i0 + lane;
-      double rs = 0.0;
-      if (i < n)
-        for (int dd = -kl; dd <= ku; ++dd) {
-          const i64 j = i + dd;
-          if (j >= 0 && j < n) rs += fabs(A[(kv + i - j) + j * ldab]);
-        }
-      anorm = fmax(anorm, rs);
+    // ---- round to FP32 (the top kl fill-in rows start at zero)
+    {
+      const i64 tot = ldab * n;
+      i64 r = tid;  // row of element e within its column, advanced without division
+      while (r >= ldab) r -= ldab;
+      for (i64 e = tid; e < tot; e += NT) {
+        A32[e] = r < kl ? 0.0f : (float)A[e];
+        r += NT;
+        while (r >= ldab) r -= ldab;
+      }
     }
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) anorm = fmax(anorm, __shfl_xor_sync(0xffffffffu, anorm, off));
-    const i64 tot = ldab * n;
-    for (i64 e = lane; e < tot; e += 32) {
-      const i64 r = e % ldab;
-      A32[e] = r < kl ? 0.0f : (float)A[e];
-    }
-    __syncwarp();
+    sync();
     // ---- FP32 factorization
-    const i64 inf = gbtrf_warp<float, 4>(n, n, kl, ku, A32, ldab, ip, smem);
-    if (lane == 0) p.info[s] = inf;
+    const i64 inf = gbtrf_group<float, 4, G>(n, n, kl, ku, A32, ldab, ip, smem);
+    if (tid == 0) p.info[s] = inf;
     int its_max = 0;
     double berr_max = 0.0;
     if (inf == 0) {
-      double* Yw = reinterpret_cast<double*>(smem);  // residual window (the factor window is free now)
-      for (i64 c = 0; c < d.nrhs; ++c) {
-        const double* b = p.B + d.b_offset + c * d.ldb;
-        double* x = p.X + d.b_offset + c * d.ldb;
-        // x0 = LU32 \ b
-        double bnorm = 0.0;
-        for (i64 i = lane; i < n; i += 32) {
-          r32[i] = (float)b[i];
-          bnorm = fmax(bnorm, fabs(b[i]));
+      const int nr_all = (int)d.nrhs;
+      const double* Bs = p.B + d.b_offset;
+      double* Xs = p.X + d.b_offset;
+      float* Rs = p.R32 + d.b_offset;  // FP32 copy of B's layout (leading dim n)
+      // x0 = LU32 \ b  for every right-hand side
+      for (i64 e = tid; e < n * nr_all; e += NT) {
+        const i64 c = e / n, i = e - c * n;
+        Rs[e] = (float)Bs[i + c * d.ldb];
+      }
+      sync();
+      gbtrs_all<float, G>(false, n, kl, ku, nr_all, A32, ldab, ip, Rs, n, smem);
+      sync();
+      for (i64 e = tid; e < n * nr_all; e += NT) {
+        const i64 c = e / n, i = e - c * n;
+        Xs[i + c * d.ldb] = (double)Rs[e];
+      }
+      sync();
+      double anorm = -1.0;  // ||A||_inf, from the first residual pass
+      // this warp's rows in the residual
+      const i64 rb = n * wig / G, re = n * (wig + 1) / G;
+      for (int c0 = 0; c0 < nr_all; c0 += kResRhs) {
+        const int nr = min(kResRhs, nr_all - c0);
+        const double* Bc = Bs + c0 * d.ldb;
+        double* Xc = Xs + c0 * d.ldb;
+        float* Rc = Rs + (i64)c0 * n;
+        double bnorm[kResRhs];
+        for (int c = 0; c < kResRhs; ++c) {
+          double bn = 0.0;
+          if (c < nr)
+            for (i64 i = tid; i < n; i += NT) bn = fmax(bn, fabs(Bc[i + c * d.ldb]));
+          bnorm[c] = grp_max<G>(bn, red);
         }
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) bnorm = fmax(bnorm, __shfl_xor_sync(0xffffffffu, bnorm, off));
-        __syncwarp();
-        gbtrs_warp<float>(false, n, kl, ku, A32, ldab, ip, r32, smem);
-        __syncwarp();
-        for (i64 i = lane; i < n; i += 32) x[i] = (double)r32[i];
-        __syncwarp();
         int it = 0;
         double be = 0.0;
         for (;;) {
-          double xnorm = 0.0;
-          const double rnorm = residual_warp(n, kl, ku, A + kl, ldab, b, x, r32, Yw, xnorm);
-          const double den = anorm * xnorm + bnorm;
-          be = den > 0.0 ? rnorm / den : rnorm;
+          double rnorm[kResRhs], xnorm[kResRhs], an = 0.0;
+          const bool first = anorm < 0.0;
+          residual_rows(n, rb, re, kl, ku, nr, A + kl, ldab, Bc, Xc, d.ldb, Rc, first, an, rnorm, xnorm);
+          if (first) anorm = grp_max<G>(an, red);
+          be = 0.0;
+          for (int c = 0; c < kResRhs; ++c) {
+            const double rn = grp_max<G>(rnorm[c], red), xn = grp_max<G>(xnorm[c], red);
+            if (c >= nr) continue;
+            const double den = anorm * xn + bnorm[c];
+            const double bc = den > 0.0 ? rn / den : rn;
+            be = (bc > be || bc != bc) ? bc : be;
+          }
           if (!(be > p.tol) || it >= p.maxit) break;  // NaN stops too
-          gbtrs_warp<float>(false, n, kl, ku, A32, ldab, ip, r32, smem);
-          __syncwarp();
-          for (i64 i = lane; i < n; i += 32) x[i] += (double)r32[i];
-          __syncwarp();
+          sync();
+          gbtrs_all<float, G>(false, n, kl, ku, nr, A32, ldab, ip, Rc, n, smem);
+          sync();
+          for (i64 e = tid; e < n * nr; e += NT) {
+            const i64 c = e / n, i = e - c * n;
+            Xc[i + c * d.ldb] += (double)Rc[e];
+          }
+          sync();
           ++it;
         }
         its_max = max(its_max, it);
-        berr_max = fmax(berr_max, be);
+        berr_max = (be > berr_max || be != be) ? be : berr_max;
       }
     }
-    if (lane == 0) {
+    if (tid == 0) {
       p.iters[s] = its_max;
       p.berr[s] = berr_max;
     }
-    __syncwarp();
+    sync();
   }
 }
 
@@ -197,27 +244,36 @@ static int dsgbsv_batched_impl(const MixedParams& p0, i64 max_kl, i64 max_ku, cu
   if (p.count == 0) return BM_OK;
   const int kl = (int)max_kl, ku = (int)max_ku;
   // per-warp shared memory: FP32 factor window / FP32 solve chunk / FP64 residual window
-  const i64 f = std::max(gbtrf_smem_elems<4>(kl, ku), gbtrs_smem_elems(kl, ku));
-  const i64 rwin = 2 * (32 + kl + ku);  // doubles as floats
-  const i64 welems = ((std::max(f, rwin) + 3) / 4) * 4;
+  const i64 f = std::max(std::max(gbtrf_smem_elems<4>(kl, ku), gbtrs_smem_elems(kl, ku)), (i64)(kHdr + 16));
+  if (kl + ku + 32 > 32 * kResQ) {
+    set_error("%s: kl + ku = %d exceeds the refined solve's limit of %d", name, kl + ku, 32 * kResQ - 32);
+    return BM_ERR_UNSUPPORTED;
+  }
+  const i64 welems = ((f + 3) / 4) * 4;
   const i64 wbytes = welems * 4;
   if (wbytes > 227 * 1024) {
     set_error("%s: widest band of the batch exceeds the per-warp window limit", name);
     return BM_ERR_UNSUPPORTED;
   }
-  p.warp_elems = welems;
-  const int wpc = (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
-  const int smem = (int)(wpc * wbytes);
-  int r = cuda_status(ensure_smem((const void*)dsgbsv_batched_kernel, smem), name);
+  p.group_elems = welems;
+  const bool cta = (kl + 1) * (kl + ku + 1) >= 512;
+  const int gpc = cta ? 1 : (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
+  const int threads = cta ? 128 : 32 * gpc;
+  const int smem = (int)(gpc * wbytes);
+  const void* kfn = cta ? (const void*)dsgbsv_batched_kernel<4> : (const void*)dsgbsv_batched_kernel<1>;
+  int r = cuda_status(ensure_smem(kfn, smem), name);
   if (r) return r;
   int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsgbsv_batched_kernel, 32 * wpc, smem), name);
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem), name);
   if (r) return r;
   per_sm = std::max(per_sm, 1);
-  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(p.count, wpc));
+  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(p.count, gpc));
   r = cuda_status(cudaMemsetAsync(p.counter, 0, sizeof(int32_t), stream), name);
   if (r) return r;
-  dsgbsv_batched_kernel<<<(unsigned)grid, 32 * wpc, smem, stream>>>(p);
+  if (cta)
+    dsgbsv_batched_kernel<4><<<(unsigned)grid, threads, smem, stream>>>(p);
+  else
+    dsgbsv_batched_kernel<1><<<(unsigned)grid, threads, smem, stream>>>(p);
   return launch_status(name);
 }
 
@@ -231,7 +287,7 @@ extern "C" int bm_dsgbsv_batched(int64_t count, const bm_gb_desc* descs, const i
   p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
   p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
   p.maxit = (int)std::min<int64_t>(maxit, 1 << 20);
-  p.warp_elems = 0;
+  p.group_elems = 0;
   if (maxit < 0) return -15;
   return bm::dsgbsv_batched_impl(p, max_kl, max_ku, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched");
 }

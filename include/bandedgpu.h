@@ -139,8 +139,9 @@ int bm_sgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *orde
  * ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol or maxit corrections.  X
  * receives the solutions (B's layout), iters/berr the corrections taken and the
  * final backward error per system (max over its right-hand sides), info the FP32
- * factorization's info.  R32 is FP32 workspace of n floats per system at the
- * system's ipiv_offset; counter is one int32 of workspace.  No counterpart in the
+ * factorization's info.  R32 is FP32 workspace laid out like B but with leading
+ * dimension n (n*nrhs floats per system at its b_offset); counter is one int32 of
+ * workspace.  kl + ku <= 128 per system.  No counterpart in the
  * reference; per system it replaces lu! + ldiv! (src/banded/BandedLU.jl:90-103,
  * src/banded/linalg.jl:24-30) when the caller accepts a backward-error target. */
 int bm_dsgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const double *AB,
