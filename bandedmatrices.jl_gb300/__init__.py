@@ -15,12 +15,13 @@ from .gbmm import banded_mul, banded_mul_, gbmm, nonzero_bands, prodbandwidths
 from .linalg import ldiv, mul, mul_, mul_t_
 from .lu import BandedLU, ldiv_, lu, lu_, transpose
 from .batched import BandedBatch, lpt_order
+from .qr import BandedQR, lmul_, qr
 
 __all__ = [
     "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
-    "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order",
+    "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
 ]
 
 

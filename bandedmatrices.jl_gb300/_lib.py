@@ -43,6 +43,12 @@ SIGNATURES: dict[str, list] = {
     "bm_dgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
     "bm_sgbsv_batched": [i64, P, P, P, P, P, P, P, i64, i64, P],
     "bm_dgbsv_batched_noalloc": [i64, P, P, P, P, P, i64, i64, P],
+    "bm_dgbqrf": [i64, i64, i64, i64, P, i64, P, P],
+    "bm_sgbqrf": [i64, i64, i64, i64, P, i64, P, P],
+    "bm_dgbqr_lmul": [C, i64, i64, i64, i64, P, i64, P, i64, i64, P, i64, P],
+    "bm_sgbqr_lmul": [C, i64, i64, i64, i64, P, i64, P, i64, i64, P, i64, P],
+    "bm_dtbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_stbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
     "bm_dsgbsv_batched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, i64, i64, P],
 }
 

@@ -1,0 +1,300 @@
+// Banded Householder QR and its Q / Q' application (replaces _banded_qr! and
+// banded_qr_lmul!, src/banded/bandedqr.jl:13-28 and :38-94), plus the upper
+// triangular band solve that finishes qr(A) \ b (tbsv!, src/blas.jl:112-147, reached
+// through src/tribanded.jl:75-83).
+//
+// gbqrf: one group (one warp, or the whole CTA for wide bands) walks the columns.
+// The active part at step k is the (l+1) x (u+1) window A(k:k+l, k:k+u) (u already
+// includes the l padding bands _banded_qr adds, bandedqr.jl:2); it is kept in shared
+// memory as a ring in both dimensions, exactly like the LU window, and the row
+// entering at each step is prefetched with cp.async.  Per step:
+//   * one thread forms the reflector of column k as LinearAlgebra.reflector! does
+//     (scaled 2-norm, nu = copysign(norm, x1), x1 <- -nu, x_i <- x_i / (x1 + nu),
+//     tau = (x1 + nu) / nu), the divisions spread over the group;
+//   * every following column of the window is owned by one thread, which applies the
+//     reflector as reflectorApply! does: v = tau * (a_0 + sum_i x_i a_i) with the
+//     fma dot product in ascending i, a_0 -= v, a_i = fma(-v, x_i, a_i).
+// The results equal the oracle's restatement bit for bit.
+//
+// gbqr_lmul: Q or Q' times B, one thread per right-hand side column running the
+// reference loop (sequential fma dot products, so again bit for bit).
+#include "lu.cuh"
+
+namespace bm {
+
+template <typename T, int P, int G>
+__device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 ldd, T* __restrict__ tau,
+                            T* __restrict__ smem) {
+  constexpr int NT = Grp<G>::NT;
+  const int tid = Grp<G>::tid();
+  const int R = l + 1, K = u + 1, RS = lu_rs(l);
+  T* hdr = smem;  // hdr[0] = tau_k, hdr[1] = xi1 (x1 + nu)
+  T* W = smem + kHdr;
+  T* S = W + (i64)RS * K;
+  const i64 ncols = min(m - 1, n);
+  for (i64 e = tid; e < min(m, n); e += NT) tau[e] = T(0);
+  if (ncols <= 0) return;
+
+  // initial window: matrix rows 0..l, columns 0..u (D(i,c) = D[(u + i - c) + c*ldd])
+  for (int e = tid; e < R * K; e += NT) {
+    const int c = e / R, r = e - c * R;
+    T v = T(0);
+    if (r < m && c < n && r - c <= l && c - r <= u) v = D[(u + r - c) + (i64)c * ldd];
+    W[r + c * RS] = v;
+  }
+  auto issue_row = [&](i64 i) {
+    T* dst = S + (int)(i & (P - 1)) * K;
+    for (int c = tid; c < K; c += NT) {
+      const i64 col = i - l + c;
+      const bool ok = i < m && col < n;
+      cp_async_elem(dst + c, ok ? D + (u + l - c) + col * ldd : D, ok);
+    }
+    cp_async_commit();
+  };
+  for (int p = 0; p < P; ++p) issue_row((i64)l + 1 + p);
+  Grp<G>::sync();
+
+  int pr0 = 0, pc0 = 0;
+  for (i64 k = 0; k < ncols; ++k) {
+    const int len = (int)min((i64)(l + 1), m - k);  // reflector length
+    T* x = W + pc0 * RS;                             // logical column 0 (ring rows)
+    auto prow = [&](int r) {
+      int pr = pr0 + r;
+      return pr >= R ? pr - R : pr;
+    };
+    // ---- reflector (thread 0): scaled norm, as the oracle's nrm2
+    if (tid == 0) {
+      T scale = T(0);
+      for (int i = 0; i < len; ++i) scale = fmax(scale, fabs(x[prow(i)]));
+      T tk = T(0), xi1 = T(0);
+      if (scale != T(0) && isfinite(scale)) {
+        T ssq = T(0);
+        for (int i = 0; i < len; ++i) {
+          const T t = x[prow(i)] / scale;
+          ssq = fma(t, t, ssq);
+        }
+        const T normu = scale * sqrt(ssq);
+        const T x1 = x[pr0];
+        const T nu = copysign(normu, x1);
+        xi1 = x1 + nu;
+        x[pr0] = -nu;
+        tk = xi1 / nu;
+      } else if (scale != T(0)) {  // Inf/NaN in the column: the norm is that value
+        const T x1 = x[pr0];
+        const T nu = copysign(scale, x1);
+        xi1 = x1 + nu;
+        x[pr0] = -nu;
+        tk = xi1 / nu;
+      }
+      hdr[0] = tk;
+      hdr[1] = xi1;
+      tau[k] = tk;
+    }
+    Grp<G>::sync();
+    const T tk = hdr[0], xi1 = hdr[1];
+    if (xi1 != T(0) || tk != T(0)) {
+      for (int i = 1 + tid; i < len; i += NT) x[prow(i)] = x[prow(i)] / xi1;
+    }
+    Grp<G>::sync();
+    // ---- apply to columns k+1 .. k+min(u, n-1-k): one thread per column
+    const int nc = (int)min((i64)u, n - 1 - k);
+    for (int c = 1 + tid; c <= nc; c += NT) {
+      int pc = pc0 + c;
+      pc = pc >= K ? pc - K : pc;
+      T* a = W + pc * RS;
+      T dot = T(0);
+      for (int i = 1; i < len; ++i) dot = fma(x[prow(i)], a[prow(i)], dot);
+      const T v = tk * (a[pr0] + dot);
+      a[pr0] = a[pr0] - v;
+      for (int i = 1; i < len; ++i) a[prow(i)] = fma(-v, x[prow(i)], a[prow(i)]);
+    }
+    Grp<G>::sync();
+    // ---- row k of R and the reflector of column k are final
+    const int ncw = (int)min((i64)u, n - 1 - k);
+    for (int c = tid; c <= ncw; c += NT) {
+      int pc = pc0 + c;
+      pc = pc >= K ? pc - K : pc;
+      D[(u - c) + (k + c) * ldd] = W[pr0 + pc * RS];
+    }
+    for (int r = 1 + tid; r < len; r += NT) D[(u + r) + k * ldd] = x[prow(r)];
+    Grp<G>::sync();
+    if (k + 1 == ncols) break;
+    // ---- slide: row k+1+l enters physical row pr0, column k+1+u enters physical column pc0
+    for (int r = tid; r < R; r += NT) W[r + pc0 * RS] = T(0);
+    cp_async_wait<P - 1>();
+    Grp<G>::sync();
+    const i64 inew = k + 1 + l;
+    const T* st = S + (int)(inew & (P - 1)) * K;
+    for (int c = tid; c < K; c += NT) {
+      int pc = pc0 + 1 + c;
+      pc = pc >= K ? pc - K : pc;
+      W[pr0 + pc * RS] = st[c];
+    }
+    Grp<G>::sync();
+    issue_row(inew + P);
+    pr0 = pr0 + 1 == R ? 0 : pr0 + 1;
+    pc0 = pc0 + 1 == K ? 0 : pc0 + 1;
+  }
+  cp_async_wait<0>();
+  Grp<G>::sync();
+  // rows ncols.. of R that the loop never slid out (m <= n: the last row; the window
+  // still holds final values for rows k+1 .. k+l and their columns)
+  {
+    const i64 k = ncols - 1;
+    for (int e = tid; e < R * K; e += NT) {
+      const int c = e / R, r = e - c * R;
+      if (r == 0) continue;  // row k was written above
+      const i64 i = k + r, col = k + c;
+      if (i < m && col < n && col >= i && col - i <= u) {
+        int pr = pr0 + r;
+        pr = pr >= R ? pr - R : pr;
+        int pc = pc0 + c;
+        pc = pc >= K ? pc - K : pc;
+        D[(u + i - col) + col * ldd] = W[pr + pc * RS];
+      }
+    }
+  }
+  Grp<G>::sync();
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * G) gbqrf_kernel(i64 m, i64 n, int l, int u, T* D, i64 ldd, T* tau) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  gbqrf_group<T, 4, G>(m, n, l, u, D, ldd, tau, reinterpret_cast<T*>(smem_raw));
+}
+
+// Q*B (adjoint = false) or Q'*B (adjoint = true): thread c owns column c of B.
+template <typename T>
+__global__ void gbqr_lmul_kernel(bool adjoint, i64 m, i64 n, int l, int u, const T* __restrict__ D, i64 ldd,
+                                 const T* __restrict__ tau, i64 ntau, i64 nrhs, T* __restrict__ B, i64 ldb) {
+  const i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nrhs) return;
+  T* b = B + c * ldb;
+  const i64 kmax = min(min(m, n), ntau);
+  const int ilo = max(1, -u);
+  for (i64 t = 0; t < kmax; ++t) {
+    const i64 k = adjoint ? t : kmax - 1 - t;
+    const T* d = D + (u - k) + k * ldd;  // d[i] = D[(i - k + u), k]
+    const i64 ihi = min(k + l, m - 1);
+    T v = b[k];
+    for (i64 i = k + ilo; i <= ihi; ++i) v = fma(d[i], b[i], v);
+    v = tau[k] * v;
+    b[k] = b[k] - v;
+    for (i64 i = k + ilo; i <= ihi; ++i) b[i] = fma(-d[i], v, b[i]);
+  }
+}
+
+// Upper triangular band solve (tbsv 'U', non-unit): the gbtrs sweeps with kl = 0.
+template <typename T, int G>
+__global__ void __launch_bounds__(32 * G) tbsv_upper_kernel(bool trans, i64 n, int k, const T* A, i64 lda, T* x,
+                                                            i64 ldx, i64 nrhs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (i64 r = blockIdx.x; r * kMaxRhs < nrhs; r += gridDim.x)
+    gbtrs_all<T, G>(trans, n, 0, k, min((i64)kMaxRhs, nrhs - r * kMaxRhs), A, lda, nullptr, x + r * kMaxRhs * ldx,
+                    ldx, reinterpret_cast<T*>(smem_raw));
+}
+
+template <typename T>
+static int gbqrf_impl(i64 m, i64 n, i64 l, i64 u, T* D, i64 ldd, T* tau, cudaStream_t stream, const char* name) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (l < 0) return -3;
+  if (u < 0) return -4;
+  if (ldd < l + u + 1) return -6;
+  if (m == 0 || n == 0) return BM_OK;
+  if (!tau) return -7;
+  const i64 bytes = gbtrf_smem_elems<4>((int)l, (int)u) * (i64)sizeof(T);
+  if (bytes > 227 * 1024) {
+    set_error("%s: band (l=%lld, u=%lld) exceeds the window limit", name, (long long)l, (long long)u);
+    return BM_ERR_UNSUPPORTED;
+  }
+  if ((l + 1) * (u + 1) >= 512) {
+    int r = cuda_status(ensure_smem((const void*)gbqrf_kernel<T, 4>, (int)bytes), name);
+    if (r) return r;
+    gbqrf_kernel<T, 4><<<1, 128, (int)bytes, stream>>>(m, n, (int)l, (int)u, D, ldd, tau);
+  } else {
+    int r = cuda_status(ensure_smem((const void*)gbqrf_kernel<T, 1>, (int)bytes), name);
+    if (r) return r;
+    gbqrf_kernel<T, 1><<<1, 32, (int)bytes, stream>>>(m, n, (int)l, (int)u, D, ldd, tau);
+  }
+  return launch_status(name);
+}
+
+template <typename T>
+static int gbqr_lmul_impl(char trans, i64 m, i64 n, i64 l, i64 u, const T* D, i64 ldd, const T* tau, i64 ntau,
+                          i64 nrhs, T* B, i64 ldb, cudaStream_t stream, const char* name) {
+  const bool adj = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
+  if (!adj && !(trans == 'N' || trans == 'n')) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (l < 0) return -4;
+  if (ldd < l + std::max<i64>(u, 0) + 1) return -7;
+  if (ntau < 0) return -9;
+  if (nrhs < 0) return -10;
+  if (ldb < std::max<i64>(1, m)) return -12;
+  if (m == 0 || nrhs == 0 || ntau == 0) return BM_OK;
+  const int threads = (int)std::min<i64>(nrhs, 128);
+  gbqr_lmul_kernel<T><<<(unsigned)ceil_div(nrhs, threads), threads, 0, stream>>>(adj, m, n, (int)l, (int)u, D, ldd,
+                                                                                  tau, ntau, nrhs, B, ldb);
+  return launch_status(name);
+}
+
+template <typename T>
+static int tbsv_impl(char uplo, char trans, char diag, i64 n, i64 k, const T* A, i64 lda, T* x, i64 incx,
+                     cudaStream_t stream, const char* name) {
+  const bool upper = (uplo == 'U' || uplo == 'u');
+  if (!upper && !(uplo == 'L' || uplo == 'l')) return -1;
+  const bool tr = (trans == 'T' || trans == 't' || trans == 'C' || trans == 'c');
+  if (!tr && !(trans == 'N' || trans == 'n')) return -2;
+  if (!(diag == 'N' || diag == 'n' || diag == 'U' || diag == 'u')) return -3;
+  if (n < 0) return -4;
+  if (k < 0) return -5;
+  if (lda < k + 1) return -7;
+  if (incx == 0) return -9;
+  if (n == 0) return BM_OK;
+  if (!upper || diag == 'U' || diag == 'u' || incx != 1) {
+    set_error("%s: only uplo='U', diag='N', incx=1 are implemented (the banded QR back-substitution)", name);
+    return BM_ERR_UNSUPPORTED;
+  }
+  const i64 bytes = gbtrs_smem_elems(0, (int)k) * (i64)sizeof(T);
+  if (bytes > 227 * 1024) {
+    set_error("%s: band too wide for the staged solve", name);
+    return BM_ERR_UNSUPPORTED;
+  }
+  int r = cuda_status(ensure_smem((const void*)tbsv_upper_kernel<T, 4>, (int)bytes), name);
+  if (r) return r;
+  tbsv_upper_kernel<T, 4><<<1, 128, (int)bytes, stream>>>(tr, n, (int)k, A, lda, x, std::max<i64>(1, n), 1);
+  return launch_status(name);
+}
+
+}  // namespace bm
+
+extern "C" int bm_dgbqrf(int64_t m, int64_t n, int64_t l, int64_t u, double* AB, int64_t ldab, double* tau,
+                         bm_stream_t stream) {
+  return bm::gbqrf_impl<double>(m, n, l, u, AB, ldab, tau, reinterpret_cast<cudaStream_t>(stream), "bm_dgbqrf");
+}
+extern "C" int bm_sgbqrf(int64_t m, int64_t n, int64_t l, int64_t u, float* AB, int64_t ldab, float* tau,
+                         bm_stream_t stream) {
+  return bm::gbqrf_impl<float>(m, n, l, u, AB, ldab, tau, reinterpret_cast<cudaStream_t>(stream), "bm_sgbqrf");
+}
+extern "C" int bm_dgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const double* AB, int64_t ldab,
+                             const double* tau, int64_t ntau, int64_t nrhs, double* B, int64_t ldb,
+                             bm_stream_t stream) {
+  return bm::gbqr_lmul_impl<double>(trans, m, n, l, u, AB, ldab, tau, ntau, nrhs, B, ldb,
+                                    reinterpret_cast<cudaStream_t>(stream), "bm_dgbqr_lmul");
+}
+extern "C" int bm_sgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const float* AB, int64_t ldab,
+                             const float* tau, int64_t ntau, int64_t nrhs, float* B, int64_t ldb, bm_stream_t stream) {
+  return bm::gbqr_lmul_impl<float>(trans, m, n, l, u, AB, ldab, tau, ntau, nrhs, B, ldb,
+                                   reinterpret_cast<cudaStream_t>(stream), "bm_sgbqr_lmul");
+}
+extern "C" int bm_dtbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const double* A, int64_t lda, double* x,
+                        int64_t incx, bm_stream_t stream) {
+  return bm::tbsv_impl<double>(uplo, trans, diag, n, k, A, lda, x, incx, reinterpret_cast<cudaStream_t>(stream),
+                               "bm_dtbsv");
+}
+extern "C" int bm_stbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const float* A, int64_t lda, float* x,
+                        int64_t incx, bm_stream_t stream) {
+  return bm::tbsv_impl<float>(uplo, trans, diag, n, k, A, lda, x, incx, reinterpret_cast<cudaStream_t>(stream),
+                              "bm_stbsv");
+}

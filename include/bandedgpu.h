@@ -106,6 +106,34 @@ int bm_dgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const
 int bm_sgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const float *AB, int64_t ldab,
               const int64_t *ipiv, float *B, int64_t ldb, bm_stream_t stream);
 
+/* ------------------------------------------------------------------ QR
+ * Householder QR of the m x n band in AB, in place: AB holds the matrix with
+ * bandwidths (l, u) where u already includes the l extra bands that receive the
+ * fill of R (qr(A) widens A from (l, u0) to (l, l+u0), src/banded/bandedqr.jl:1-2);
+ * ldab >= l+u+1.  On exit the upper band holds R and the l rows below the diagonal
+ * hold the reflectors; tau (min(m,n) entries) receives their scalars, zero beyond
+ * min(m-1,n).  Reflector convention of LinearAlgebra.reflector!.  Replaces
+ * _banded_qr! (src/banded/bandedqr.jl:13-28). */
+int bm_dgbqrf(int64_t m, int64_t n, int64_t l, int64_t u, double *AB, int64_t ldab, double *tau,
+              bm_stream_t stream);
+int bm_sgbqrf(int64_t m, int64_t n, int64_t l, int64_t u, float *AB, int64_t ldab, float *tau, bm_stream_t stream);
+
+/* B <- Q*B (trans 'N') or Q'*B ('T'/'C') with the bm_*gbqrf factors (m x n,
+ * bandwidths (l,u), ntau reflectors); B is m x nrhs, leading dim ldb.  Replaces
+ * banded_qr_lmul! (src/banded/bandedqr.jl:38-94). */
+int bm_dgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const double *AB, int64_t ldab,
+                  const double *tau, int64_t ntau, int64_t nrhs, double *B, int64_t ldb, bm_stream_t stream);
+int bm_sgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const float *AB, int64_t ldab,
+                  const float *tau, int64_t ntau, int64_t nrhs, float *B, int64_t ldb, bm_stream_t stream);
+
+/* Triangular band solve op(A) x = b, BLAS xTBSV; uplo 'U', diag 'N', incx 1 (the
+ * case banded QR's back-substitution uses).  Replaces tbsv! (src/blas.jl:112-147)
+ * reached from UpperTriangular(R) \ b (src/tribanded.jl:75-83). */
+int bm_dtbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const double *A, int64_t lda, double *x,
+             int64_t incx, bm_stream_t stream);
+int bm_stbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const float *A, int64_t lda, float *x,
+             int64_t incx, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ batched
  * One square system of a batch: its band (gbtrf storage) at AB + ab_offset, its
  * right-hand sides at B + b_offset (n x nrhs, leading dim ldb), its pivots at
