@@ -16,12 +16,15 @@ from .linalg import ldiv, mul, mul_, mul_t_
 from .lu import BandedLU, ldiv_, lu, lu_, transpose
 from .batched import BandedBatch, lpt_order
 from .qr import BandedQR, lmul_, qr
+from .autograd import BandedSolve, banded_solve
+from . import pde
 
 __all__ = [
     "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
+    "BandedSolve", "banded_solve",
 ]
 
 

@@ -49,6 +49,8 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbqr_lmul": [C, i64, i64, i64, i64, P, i64, P, i64, i64, P, i64, P],
     "bm_dtbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
     "bm_stbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_dgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
+    "bm_sgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
     "bm_dsgbsv_batched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, i64, i64, P],
 }
 

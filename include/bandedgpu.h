@@ -134,6 +134,22 @@ int bm_dtbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const doubl
 int bm_stbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const float *A, int64_t lda, float *x,
              int64_t incx, bm_stream_t stream);
 
+/* ------------------------------------------------------------------ adjoint
+ * Reverse-mode derivative of X = A \ B for an upstream gradient W = dL/dX (all
+ * n x nrhs, leading dim n), with A's xGBTRF factors (LU, ldab, ipiv):
+ *   grad_B    <- A^{-T} W                      (transposed xGBTRS on the factors)
+ *   grad_band <- -(A^{-T} W) X^T on A's band   (BLAS band layout, (kl+ku+1) x n,
+ *                                               leading dim ldg; NULL to skip)
+ * X may be NULL: it is then recomputed from B into Xwork (n x nrhs workspace).  No
+ * counterpart in the reference; it is the rrule of \ built on the transposed solve
+ * ldiv!(transpose(F), B) (src/banded/linalg.jl:41-47). */
+int bm_dgbsv_adjoint(int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double *LU, int64_t ldab,
+                     const int64_t *ipiv, const double *X, const double *B, const double *W, double *grad_B,
+                     double *grad_band, int64_t ldg, double *Xwork, bm_stream_t stream);
+int bm_sgbsv_adjoint(int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const float *LU, int64_t ldab,
+                     const int64_t *ipiv, const float *X, const float *B, const float *W, float *grad_B,
+                     float *grad_band, int64_t ldg, float *Xwork, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ batched
  * One square system of a batch: its band (gbtrf storage) at AB + ab_offset, its
  * right-hand sides at B + b_offset (n x nrhs, leading dim ldb), its pivots at
