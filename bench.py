@@ -377,6 +377,177 @@ def run_e2e(bm, gb, mm, dev, stream, steps):
             "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps}
 
 
+# --------------------------------------------------------------------- other workloads
+def _timed(fn, stream, reps=1, restore=None):
+    import torch
+
+    ts = []
+    for _ in range(reps):
+        if restore:
+            restore()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return min(ts)
+
+
+def batched_config(n_sys=4096, seed=3):
+    """4096 systems: n log-uniform in [256,16384], l,u uniform in [1,64], 1-8 right-hand sides."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(256), np.log(16384), n_sys)).astype(np.int64)
+    kl = rng.integers(1, 65, n_sys)
+    ku = rng.integers(1, 65, n_sys)
+    nrhs = rng.integers(1, 9, n_sys)
+    return n, kl, ku, nrhs
+
+
+def run_batched(bm, dev, stream):
+    """Plain FP64 factor+solve vs FP32-factor/FP64-refined solve of the same batch."""
+    import numpy as np
+    import torch
+
+    n, kl, ku, nrhs = batched_config()
+    batch = bm.BandedBatch(n, kl, ku, nrhs, torch.float64, dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    for s in range(batch.count):
+        mb = batch.matrix_band(s)
+        mb.normal_(generator=g)
+        mb[int(ku[s])] += 2.0 * (kl[s] + ku[s])
+        batch.rhs(s).normal_(generator=g)
+    AB0, B0 = batch.AB.clone(), batch.B.clone()
+
+    def restore():
+        batch.AB.copy_(AB0)
+        batch.B.copy_(B0)
+
+    restore()
+    batch.factor_solve()  # warm-up (device set-up)
+    t_plain = _timed(batch.factor_solve, stream, reps=2, restore=restore)
+    # backward error of the plain solutions on a sample of systems (FP64 residual on the GPU)
+    berr_plain = 0.0
+    for s in range(0, batch.count, 256):
+        A = bm.BandedMatrix(AB0[int(batch.ab_off[s]): int(batch.ab_off[s] + batch.ldab[s] * batch.n[s])]
+                            .view(int(batch.n[s]), int(batch.ldab[s])).t()[int(kl[s]):], int(n[s]), int(kl[s]),
+                            int(ku[s]))
+        X = batch.rhs(s)
+        Bs = B0[int(batch.b_off[s]): int(batch.b_off[s] + n[s] * nrhs[s])].view(int(nrhs[s]), int(n[s])).t()
+        absA = bm.BandedMatrix(A.data.abs().contiguous().t().contiguous().t(), A.m, A.l, A.u)
+        an = (absA @ torch.ones(A.n, dtype=torch.float64, device=dev)).max().item()
+        for c in range(int(nrhs[s])):
+            r = Bs[:, c].contiguous()
+            bm.mul_(r, A, X[:, c].contiguous(), -1.0, 1.0)
+            be = r.abs().max().item() / (an * X[:, c].abs().max().item() + Bs[:, c].abs().max().item())
+            berr_plain = max(berr_plain, be)
+    restore()
+    batch.solve_mixed(1e-10, 30)
+    t_mixed = _timed(lambda: batch.solve_mixed(1e-10, 30), stream, reps=2)
+    its = batch.iters.cpu().numpy()
+    flops = float((n * (2 * kl * (kl + ku) + kl) + nrhs * 2 * n * (2 * kl + ku + 1)).sum())
+    return {
+        "workload": "4096 systems, n log-uniform [256,16384], l,u uniform [1,64], 1-8 RHS, randn + 2(l+u) I",
+        "plain_fp64": {"ms": t_plain, "systems_per_s": batch.count / (t_plain / 1e3),
+                       "gflops": flops / (t_plain / 1e3) / 1e9, "max_berr_sampled": berr_plain},
+        "mixed_fp32_fp64_refined": {"ms": t_mixed, "systems_per_s": batch.count / (t_mixed / 1e3),
+                                    "tol": 1e-10, "max_berr": float(batch.berr.max().item()),
+                                    "iters_max": int(its.max()), "iters_mean": float(its.mean())},
+        "speedup_mixed_vs_plain": t_plain / t_mixed,
+        "launches_per_solve": 1,
+    }
+
+
+def run_cpu_runnable(bm, dev, stream):
+    """brandn(10000,10000,4,3) + 10I: A*b, A*A and A\\b latencies on the GPU."""
+    import torch
+
+    n, l, u = 10000, 4, 3
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    A = bm.brandn(torch.float64, n, n, l, u, device=dev, generator=g)
+    A.data[u] += 10.0
+    b = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+    y = torch.empty(n, dtype=torch.float64, device=dev)
+    C = bm.BandedMatrix.zeros((n, n), (2 * l, 2 * u), torch.float64, dev)
+    for _ in range(3):
+        bm.mul_(y, A, b)
+        bm.banded_mul_(C, A, A)
+        x = A.solve(b)
+    t_mv = _timed(lambda: bm.mul_(y, A, b), stream, reps=5)
+    t_mm = _timed(lambda: bm.banded_mul_(C, A, A), stream, reps=5)
+    t_sv = _timed(lambda: A.solve(b), stream, reps=5)
+    return {"workload": "n=10000, (l,u)=(4,3), f64, randn + 10 I", "gbmv_us": t_mv * 1e3, "gbmm_us": t_mm * 1e3,
+            "lu_solve_us": t_sv * 1e3}
+
+
+def run_qr(bm, dev, stream):
+    """Banded QR least-squares solve, n = 2^18, l = u = 32, with an FP64 residual check."""
+    import torch
+
+    n, l, u = 1 << 18, 32, 32
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    A = bm.BandedMatrix(bm.band_storage(l + u + 1, n, torch.float64, dev), n, l, u)
+    A.data.normal_(generator=g)
+    b = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+    F = bm.qr(A)
+    out = {}
+    t_f = _timed(lambda: out.__setitem__("F", bm.qr(A)), stream)
+    t_s = _timed(lambda: out.__setitem__("x", out["F"].solve(b)), stream)
+    x = out["x"]
+    r = b.clone()
+    bm.mul_(r, A, x, -1.0, 1.0)
+    absA = bm.BandedMatrix(A.data.abs(), n, l, u)
+    an = (absA @ torch.ones(n, dtype=torch.float64, device=dev)).max().item()
+    berr = r.abs().max().item() / (an * x.abs().max().item() + b.abs().max().item())
+    del F
+    return {"workload": "qr(A) \\ b, n=2^18, l=u=32, f64 randn", "factor_ms": t_f, "solve_ms": t_s,
+            "gflops_factor": 4.0 * n * (l + 1) * (2 * l + u) / (t_f / 1e3) / 1e9, "berr": berr}
+
+
+def run_pde(bm, dev, stream, G=96):
+    """Differentiated PDE solve: 5-point variable-coefficient diffusion on a G x G grid,
+    x = A \\ b, L = w.x, adjoint dL/db and dL/dA; directional central difference h = 1e-6."""
+    import numpy as np
+    import torch
+
+    kcell = np.exp(bm.pde.gaussian_field(G, 16.0, seed=11))
+    A = bm.pde.diffusion_band(kcell, torch.float64, dev)
+    n = G * G
+    rng = np.random.default_rng(12)
+    b = torch.from_numpy(rng.standard_normal(n)).to(dev)
+    w = torch.from_numpy(rng.standard_normal(n)).to(dev)
+    D = A.data.clone().requires_grad_(True)
+    bt = b.clone().requires_grad_(True)
+    st = {}
+
+    def fwd():
+        st["x"] = bm.banded_solve(D, bt, G, G)
+
+    def bwd():
+        (st["x"] * w).sum().backward()
+
+    fwd()
+    bwd()
+    D.grad = None
+    bt.grad = None
+    t_f = _timed(fwd, stream)
+    t_b = _timed(bwd, stream)
+    h = 1e-6
+    dD = torch.from_numpy(rng.standard_normal(tuple(A.data.shape))).to(dev) * (A.data != 0)
+    db = torch.from_numpy(rng.standard_normal(n)).to(dev)
+    L = lambda d, bb: float((bm.banded_solve(d, bb, G, G) * w).sum())
+    fd = (L(A.data + h * dD, b + h * db) - L(A.data - h * dD, b - h * db)) / (2 * h)
+    ad = float((D.grad * dD).sum() + (bt.grad * db).sum())
+    return {"workload": f"5-point diffusion, {G}x{G} grid (n={n}, l=u={G}), exp(GRF, corr 16), f64",
+            "forward_ms": t_f, "adjoint_ms": t_b, "fd_rel_err": abs(fd - ad) / max(1.0, abs(fd))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,6 +555,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep-only", action="store_true", help="time only the gbmv/gbmm sweep")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -408,6 +580,18 @@ def main():
 
         dist.init_process_group("nccl")
     out = run_gpu(args, rank, world)
+    if rank == 0 and not args.sweep_only:
+        import torch
+
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+        stream = torch.cuda.current_stream(dev)
+        bm = __import__("__graft_entry__").package()
+        out["batched_solve"] = run_batched(bm, dev, stream)
+        torch.cuda.empty_cache()
+        out["cpu_runnable"] = run_cpu_runnable(bm, dev, stream)
+        out["qr_least_squares"] = run_qr(bm, dev, stream)
+        torch.cuda.empty_cache()
+        out["pde_adjoint"] = run_pde(bm, dev, stream)
     if rank == 0:
         if not args.no_cpu_baseline:
             cb = cpu_sweep(1, 1)
