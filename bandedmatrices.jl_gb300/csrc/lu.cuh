@@ -69,6 +69,39 @@ __device__ __forceinline__ double grp_max(double v, double* scratch) {
   return v;
 }
 
+// |a| as an integer key whose order is the order of |a| (IEEE bit pattern, sign cleared).
+__device__ __forceinline__ unsigned long long abs_key(double a) {
+  return (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long abs_key(float a) {
+  return (unsigned long long)(__float_as_uint(a) & 0x7fffffffu);
+}
+// The key idamax's scan compares: |a| by bit pattern, except that a NaN never wins
+// (both |x| > NaN and NaN > |x| are false in the scan) unless it is the first entry,
+// which the scan starts from and nothing then exceeds.
+__device__ __forceinline__ unsigned long long pivot_key(double a, bool first) {
+  const unsigned long long k = abs_key(a);
+  return k > 0x7ff0000000000000ull ? (first ? ~0ull : 0ull) : k;
+}
+__device__ __forceinline__ unsigned long long pivot_key(float a, bool first) {
+  const unsigned long long k = abs_key(a);
+  return k > 0x7f800000ull ? (first ? ~0ull : 0ull) : k;
+}
+// a != 0 (either sign of zero) without a floating-point compare
+__device__ __forceinline__ bool is_nonzero(double a) { return (abs_key(a)) != 0ull; }
+__device__ __forceinline__ bool is_nonzero(float a) { return (abs_key(a)) != 0ull; }
+
+// Warp argmax with the first index winning ties (idamax): every lane passes its best
+// (key, index); lanes with nothing to offer pass index 0x7fffffff.  Returns the winning
+// index to all lanes, using redux.sync on the integer pipe.
+__device__ __forceinline__ int warp_argmax_first(unsigned long long key, int idx) {
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+  const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+  const bool cand = (hi == mhi) && (lo == mlo);
+  return (int)__reduce_min_sync(0xffffffffu, cand ? (unsigned)idx : 0x7fffffffu);
+}
+
 // ------------------------------------------------------------ cp.async helpers
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T* dst, const T* src, bool valid) {
@@ -170,123 +203,127 @@ __device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64
   i64 ju = 0;
   for (i64 j = 0; j < mn; ++j) {
     const int km = (int)min((i64)kl, m - 1 - j);
-    // ---- pivot (warp 0): first index of max |a| over logical rows 0..km of column 0
+    // ---- pivot (warp 0): first index of the largest |a| over logical rows 0..km of
+    // column 0.  |a| is compared through its IEEE bit pattern (monotone for |a| >= 0), so
+    // the search runs on the integer pipe: a per-lane scan, then redux.sync max/min.
     int jp = 0;
+    T piv = T(0), old0 = T(0);
     if (wig == 0) {
-      T best = T(-1);
-      int bidx = 0x7fffffff;
+      unsigned long long key = 0ull;
+      int idx = 0x7fffffff;
       for (int r = lane; r <= km; r += 32) {
         int pr = pr0 + r;
         pr = pr >= R ? pr - R : pr;
-        const T v = fabs(W[pr + pc0 * RS]);
-        if (bidx == 0x7fffffff || v > best) {
-          best = v;
-          bidx = r;
+        const unsigned long long k = pivot_key(W[pr + pc0 * RS], r == 0);
+        if (idx == 0x7fffffff || k > key) {
+          key = k;
+          idx = r;
         }
       }
-#pragma unroll
-      for (int off = 16; off >= 1; off >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, best, off);
-        const int oi = __shfl_down_sync(0xffffffffu, bidx, off);
-        if (lane + off < 32 && (ov > best || (ov == best && oi < bidx))) {
-          best = ov;
-          bidx = oi;
-        }
-      }
-      jp = __shfl_sync(0xffffffffu, bidx, 0);
+      jp = warp_argmax_first(key, idx);
+      int pp = pr0 + jp;
+      pp = pp >= R ? pp - R : pp;
+      piv = W[pp + pc0 * RS];
+      old0 = W[pr0 + pc0 * RS];  // row j's entry, moves to row j+jp by the interchange
       if (lane == 0) {
         ipiv[j] = j + jp + 1;
-        if (G > 1) hdr[0] = jp;
+        if (G > 1) {
+          hdr[0] = jp;
+          smem[2] = piv;  // T slots 2, 3 lie past the two int slots of the header
+          smem[3] = old0;
+        }
       }
     }
+    // every thread holds jp, piv and old0 before any thread overwrites column 0
+    Grp<G>::sync();
     if (G > 1) {
-      Grp<G>::sync();
       jp = hdr[0];
+      piv = smem[2];
+      old0 = smem[3];
     }
     int prp = pr0 + jp;
     prp = prp >= R ? prp - R : prp;
-    const T piv = W[prp + pc0 * RS];
-    if (piv != T(0)) {
+    const bool nonsingular = is_nonzero(piv);
+    int nc = 0;
+    if (nonsingular) {
       ju = max(ju, min(j + ku + jp, n - 1));
-      const int nc = (int)(ju - j);
-      if (jp != 0) {
-        for (int c = tid; c <= nc; c += NT) {
-          int pc = pc0 + c;
-          pc = pc >= K ? pc - K : pc;
-          const T t = W[pr0 + pc * RS];
-          W[pr0 + pc * RS] = W[prp + pc * RS];
-          W[prp + pc * RS] = t;
-        }
-        Grp<G>::sync();
-      }
+      nc = (int)(ju - j);
+      // ---- interchange in column 0 and scaling by the reciprocal of the pivot (dscal)
       if (km > 0) {
         const T rcp = T(1) / piv;
         for (int r = 1 + tid; r <= km; r += NT) {
           int pr = pr0 + r;
           pr = pr >= R ? pr - R : pr;
-          W[pr + pc0 * RS] = rcp * W[pr + pc0 * RS];
+          const T v = (r == jp) ? old0 : W[pr + pc0 * RS];
+          W[pr + pc0 * RS] = rcp * v;
         }
-        Grp<G>::sync();
-        // rank-1 update: threads own columns; rows go in chunks of kU so that a chunk's
-        // shared-memory loads are all in flight before its stores
-        constexpr int kU = 8;
-        const T* col0 = W + pc0 * RS;
-        for (int c = 1 + tid; c <= nc; c += NT) {
-          int pc = pc0 + c;
-          pc = pc >= K ? pc - K : pc;
-          T* colc = W + pc * RS;
-          const T uc = colc[pr0];
-          if (uc != T(0)) {
-            const T t = -uc;
-            int pr = pr0;
-            for (int r0 = 1; r0 <= km; r0 += kU) {
-              T mv[kU], av[kU];
-              int pq[kU];
+      } else if (jp != 0 && tid == 0) {
+        W[prp + pc0 * RS] = old0;
+      }
+      if (tid == 0) W[pr0 + pc0 * RS] = piv;
+      Grp<G>::sync();
+      // ---- per column c = 1..nc (one owner thread): interchange rows 0 and jp, then the
+      // rank-1 update a <- fma(l_r, -u_c, a) (dger, skipping u_c == 0).  Rows go in chunks
+      // of kU so that a chunk's shared-memory loads are in flight before its stores.
+      constexpr int kU = 8;
+      const T* col0 = W + pc0 * RS;
+      for (int c = 1 + tid; c <= nc; c += NT) {
+        int pc = pc0 + c;
+        pc = pc >= K ? pc - K : pc;
+        T* colc = W + pc * RS;
+        T uc = colc[pr0];
+        if (jp != 0) {
+          const T t = colc[prp];
+          colc[prp] = uc;
+          colc[pr0] = t;
+          uc = t;
+        }
+        if (km > 0 && is_nonzero(uc)) {
+          int pr = pr0;
+          for (int r0 = 1; r0 <= km; r0 += kU) {
+            T mv[kU], av[kU];
+            int pq[kU];
 #pragma unroll
-              for (int q = 0; q < kU; ++q) {
-                pr = pr + 1 == R ? 0 : pr + 1;
-                pq[q] = pr;
-                if (r0 + q <= km) {
-                  mv[q] = col0[pr];
-                  av[q] = colc[pr];
-                }
+            for (int q = 0; q < kU; ++q) {
+              pr = pr + 1 == R ? 0 : pr + 1;
+              pq[q] = pr;
+              if (r0 + q <= km) {
+                mv[q] = col0[pr];
+                av[q] = colc[pr];
               }
-#pragma unroll
-              for (int q = 0; q < kU; ++q)
-                if (r0 + q <= km) colc[pq[q]] = fma(mv[q], t, av[q]);
             }
+#pragma unroll
+            for (int q = 0; q < kU; ++q)
+              if (r0 + q <= km) colc[pq[q]] = fma(mv[q], -uc, av[q]);
           }
         }
-        Grp<G>::sync();
       }
     } else if (info == 0) {
       info = j + 1;
     }
-    // ---- U row j (logical row 0) and L column j are final
-    const int ncw = (int)min((i64)kv, n - 1 - j);
-    for (int c = tid; c <= ncw; c += NT) {
-      int pc = pc0 + c;
-      pc = pc >= K ? pc - K : pc;
-      ab[(kv - c) + (j + c) * ldab] = W[pr0 + pc * RS];
-    }
-    for (int r = 1 + tid; r <= km; r += NT) {
-      int pr = pr0 + r;
-      pr = pr >= R ? pr - R : pr;
-      ab[(kv + r) + j * ldab] = W[pr + pc0 * RS];
-    }
+    const bool last = (j + 1 == mn);
+    if (!last) cp_async_wait<P - 1>();
     Grp<G>::sync();
-    if (j + 1 == mn) break;
-    // ---- slide: row j+1+kl enters physical row pr0, column j+1+kv enters physical column pc0
-    for (int r = tid; r < R; r += NT) W[r + pc0 * RS] = T(0);
-    cp_async_wait<P - 1>();
-    Grp<G>::sync();
+    // ---- write-back and slide, fused: the thread owning logical column c stores row j's
+    // entry (U(j, j+c)) and puts the entering row's value for that physical column in its
+    // place (column c becomes logical c-1; column 0 becomes logical kv, the new column);
+    // the thread owning row r of column 0 stores L(j+r, j) and zeroes the slot (fill-in).
     const i64 inew = j + 1 + kl;
     const T* st = S + (int)(inew & (P - 1)) * K;
+    const int ncw = (int)min((i64)kv, n - 1 - j);
     for (int c = tid; c < K; c += NT) {
-      int pc = pc0 + 1 + c;
+      int pc = pc0 + c;
       pc = pc >= K ? pc - K : pc;
-      W[pr0 + pc * RS] = st[c];
+      if (c <= ncw) ab[(kv - c) + (j + c) * ldab] = W[pr0 + pc * RS];
+      if (!last) W[pr0 + pc * RS] = st[c == 0 ? kv : c - 1];
     }
+    for (int r = 1 + tid; r <= kl; r += NT) {
+      int pr = pr0 + r;
+      pr = pr >= R ? pr - R : pr;
+      if (r <= km) ab[(kv + r) + j * ldab] = W[pr + pc0 * RS];
+      W[pr + pc0 * RS] = T(0);
+    }
+    if (last) break;
     Grp<G>::sync();
     issue_row(inew + P);
     pr0 = pr0 + 1 == R ? 0 : pr0 + 1;

@@ -8,12 +8,15 @@
 // includes the l padding bands _banded_qr adds, bandedqr.jl:2); it is kept in shared
 // memory as a ring in both dimensions, exactly like the LU window, and the row
 // entering at each step is prefetched with cp.async.  Per step:
-//   * one thread forms the reflector of column k as LinearAlgebra.reflector! does
-//     (scaled 2-norm, nu = copysign(norm, x1), x1 <- -nu, x_i <- x_i / (x1 + nu),
-//     tau = (x1 + nu) / nu), the divisions spread over the group;
-//   * every following column of the window is owned by one thread, which applies the
-//     reflector as reflectorApply! does: v = tau * (a_0 + sum_i x_i a_i) with the
-//     fma dot product in ascending i, a_0 -= v, a_i = fma(-v, x_i, a_i).
+//   * warp 0 forms the reflector of column k as LinearAlgebra.reflector! does
+//     (2-norm, nu = copysign(norm, x1), x1 <- -nu, x_i <- x_i / (x1 + nu),
+//     tau = (x1 + nu) / nu), the divisions spread over the group.  The norm is the
+//     one a SIMD BLAS nrm2 forms: max|x| first; squares of x itself when max|x| lies
+//     in [2^-400, 2^400] (f32: [2^-50, 2^50]), else of x / max|x|, summed in four
+//     interleaved fma partial sums combined as (s0 + s1) + (s2 + s3);
+//   * every following column of the window is shared by four threads, which apply the
+//     reflector as reflectorApply! does: v = tau * (a_0 + x'a) with the dot product in
+//     the same four-way interleaved order, a_0 -= v, a_i = fma(-v, x_i, a_i).
 // The results equal the oracle's restatement bit for bit.
 //
 // gbqr_lmul: Q or Q' times B, one thread per right-hand side column running the
@@ -62,33 +65,47 @@ __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 l
       int pr = pr0 + r;
       return pr >= R ? pr - R : pr;
     };
-    // ---- reflector (thread 0): scaled norm, as the oracle's nrm2
-    if (tid == 0) {
-      T scale = T(0);
-      for (int i = 0; i < len; ++i) scale = fmax(scale, fabs(x[prow(i)]));
-      T tk = T(0), xi1 = T(0);
-      if (scale != T(0) && isfinite(scale)) {
-        T ssq = T(0);
-        for (int i = 0; i < len; ++i) {
-          const T t = x[prow(i)] / scale;
-          ssq = fma(t, t, ssq);
-        }
-        const T normu = scale * sqrt(ssq);
-        const T x1 = x[pr0];
-        const T nu = copysign(normu, x1);
-        xi1 = x1 + nu;
-        x[pr0] = -nu;
-        tk = xi1 / nu;
-      } else if (scale != T(0)) {  // Inf/NaN in the column: the norm is that value
-        const T x1 = x[pr0];
-        const T nu = copysign(scale, x1);
-        xi1 = x1 + nu;
-        x[pr0] = -nu;
-        tk = xi1 / nu;
+    // ---- reflector (warp 0).  max|x| through integer keys; the sum of squares in four
+    // interleaved partial sums (lane t takes rows t, t+4, ...), combined (s0+s1)+(s2+s3);
+    // squares taken directly when max|x| is in a safe range, else of x/max|x|.
+    if (tid < 32) {
+      const int lane = tid;
+      unsigned long long key = 0ull;
+      for (int i = lane; i < len; i += 32) {
+        const unsigned long long kk = pivot_key(x[prow(i)], false);  // NaN never raises the scale
+        key = kk > key ? kk : key;
       }
-      hdr[0] = tk;
-      hdr[1] = xi1;
-      tau[k] = tk;
+      const unsigned mhi = __reduce_max_sync(0xffffffffu, (unsigned)(key >> 32));
+      const unsigned mlo = __reduce_max_sync(0xffffffffu, (unsigned)(key >> 32) == mhi ? (unsigned)key : 0u);
+      const unsigned long long mkey = ((unsigned long long)mhi << 32) | mlo;
+      T scale;
+      if constexpr (sizeof(T) == 8) scale = __longlong_as_double((long long)mkey);
+      else scale = __uint_as_float((unsigned)mkey);
+      const bool finite_nz = scale != T(0) && isfinite(scale);
+      const bool direct = sizeof(T) == 8 ? (scale > T(0x1p-400) && scale < T(0x1p400))
+                                         : (scale > T(0x1p-50) && scale < T(0x1p50));
+      T part = T(0);
+      if (finite_nz && lane < 4)
+        for (int i = lane; i < len; i += 4) {
+          const T t = direct ? x[prow(i)] : x[prow(i)] / scale;
+          part = fma(t, t, part);
+        }
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      if (lane == 0) {
+        T tk = T(0), xi1 = T(0);
+        if (scale != T(0)) {
+          const T normu = !finite_nz ? scale : (direct ? sqrt(part) : scale * sqrt(part));
+          const T x1 = x[pr0];
+          const T nu = copysign(normu, x1);
+          xi1 = x1 + nu;
+          x[pr0] = -nu;
+          tk = xi1 / nu;
+        }
+        hdr[0] = tk;
+        hdr[1] = xi1;
+        tau[k] = tk;
+      }
     }
     Grp<G>::sync();
     const T tk = hdr[0], xi1 = hdr[1];
@@ -96,17 +113,28 @@ __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 l
       for (int i = 1 + tid; i < len; i += NT) x[prow(i)] = x[prow(i)] / xi1;
     }
     Grp<G>::sync();
-    // ---- apply to columns k+1 .. k+min(u, n-1-k): one thread per column
+    // ---- apply to columns k+1 .. k+min(u, n-1-k): four threads per column, the dot
+    // product in four interleaved partial sums (rows 1+t, 5+t, ...) combined
+    // (s0+s1)+(s2+s3), then each thread updates its own rows
     const int nc = (int)min((i64)u, n - 1 - k);
-    for (int c = 1 + tid; c <= nc; c += NT) {
+    const int sub = tid & 3;
+    for (int base = 0; base < nc; base += NT / 4) {
+      const int c = 1 + base + (tid >> 2);
+      const bool act = c <= nc;
       int pc = pc0 + c;
       pc = pc >= K ? pc - K : pc;
-      T* a = W + pc * RS;
-      T dot = T(0);
-      for (int i = 1; i < len; ++i) dot = fma(x[prow(i)], a[prow(i)], dot);
-      const T v = tk * (a[pr0] + dot);
-      a[pr0] = a[pr0] - v;
-      for (int i = 1; i < len; ++i) a[prow(i)] = fma(-v, x[prow(i)], a[prow(i)]);
+      T* a = W + (act ? pc : pc0) * RS;
+      const T a0 = act ? a[pr0] : T(0);
+      T part = T(0);
+      if (act)
+        for (int i = 1 + sub; i < len; i += 4) part = fma(x[prow(i)], a[prow(i)], part);
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      if (act) {
+        const T v = tk * (a0 + part);
+        if (sub == 0) a[pr0] = a0 - v;
+        for (int i = 1 + sub; i < len; i += 4) a[prow(i)] = fma(-v, x[prow(i)], a[prow(i)]);
+      }
     }
     Grp<G>::sync();
     // ---- row k of R and the reflector of column k are final

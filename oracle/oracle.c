@@ -305,15 +305,34 @@ int P##gbmm_percol(i64 n, i64 nu, i64 m, i64 Al, i64 Au, i64 Bl, i64 Bu,        
     return 0;                                                                                   \
 }                                                                                               \
                                                                                                 \
-/* Euclidean norm, scaled (overflow-safe) two-pass form.                                       */ \
+/* Euclidean norm (BLAS xNRM2, which LinearAlgebra.norm calls for strided vectors).    */ \
+/* Squares are summed in four interleaved partial sums (element i goes to sum i mod 4,  */ \
+/* each accumulated with fma in ascending i), combined as (s0+s1)+(s2+s3), the order of */ \
+/* a 4-lane SIMD kernel.  When max|x| is inside a safe range the squares are taken      */ \
+/* directly; otherwise each element is first divided by max|x| (overflow-safe).         */ \
 static T P##nrm2(const T *x, i64 n)                                                             \
 {                                                                                               \
     T scale = 0;                                                                                \
     for (i64 i = 0; i < n; i++) if (ABS(x[i]) > scale) scale = ABS(x[i]);                       \
     if (scale == 0 || !isfinite(scale)) return scale;                                           \
-    T ssq = 0;                                                                                  \
-    for (i64 i = 0; i < n; i++) { T t = x[i] / scale; ssq = FMA(t, t, ssq); }                   \
-    return scale * SQRT(ssq);                                                                   \
+    const int direct = (sizeof(T) == 8) ? (scale > 0x1p-400 && scale < 0x1p400)                 \
+                                        : (scale > 0x1p-50f && scale < 0x1p50f);                \
+    T s4[4] = {0, 0, 0, 0};                                                                     \
+    for (i64 i = 0; i < n; i++) {                                                               \
+        T t = direct ? x[i] : x[i] / scale;                                                     \
+        s4[i & 3] = FMA(t, t, s4[i & 3]);                                                       \
+    }                                                                                           \
+    T ssq = (s4[0] + s4[1]) + (s4[2] + s4[3]);                                                  \
+    return direct ? SQRT(ssq) : scale * SQRT(ssq);                                              \
+}                                                                                               \
+                                                                                                \
+/* Dot product of x[1..len) and a[1..len) (BLAS xDOT, called by reflectorApply!): four   */ \
+/* interleaved partial sums (element i to sum (i-1) mod 4), combined as (s0+s1)+(s2+s3). */ \
+static T P##dot4(const T *x, const T *a, i64 len)                                               \
+{                                                                                               \
+    T s4[4] = {0, 0, 0, 0};                                                                     \
+    for (i64 i = 1; i < len; i++) s4[(i - 1) & 3] = FMA(x[i], a[i], s4[(i - 1) & 3]);          \
+    return (s4[0] + s4[1]) + (s4[2] + s4[3]);                                                   \
 }                                                                                               \
                                                                                                 \
 /* LinearAlgebra.reflector!: x[0] <- -nu, x[1:] <- x[1:]/(xi1+nu), returns tau = (xi1+nu)/nu   */ \
@@ -347,9 +366,7 @@ int P##gbqrf(i64 m, i64 n, i64 l, i64 u, T *D, i64 ldd, T *tau)                 
         tau[k] = tk;                                                                            \
         for (i64 j = 1; j <= imin(u, n - (k + 1)); j++) {                                       \
             T *aj = D + (u - j) + (k + j) * ldd; /* same length as x */                         \
-            T dot = 0;                                                                          \
-            for (i64 i = 1; i < len; i++) dot = FMA(x[i], aj[i], dot);                          \
-            T vAj = tk * (aj[0] + dot);                                                         \
+            T vAj = tk * (aj[0] + P##dot4(x, aj, len));                                         \
             aj[0] = aj[0] - vAj;                                                                \
             for (i64 i = 1; i < len; i++) aj[i] = FMA(-vAj, x[i], aj[i]);                        \
         }                                                                                       \
