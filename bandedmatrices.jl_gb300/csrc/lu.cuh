@@ -102,22 +102,6 @@ __device__ __forceinline__ int warp_argmax_first(unsigned long long key, int idx
   return (int)__reduce_min_sync(0xffffffffu, cand ? (unsigned)idx : 0x7fffffffu);
 }
 
-// ------------------------------------------------------------ cp.async helpers
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T* dst, const T* src, bool valid) {
-  const uint32_t d = smem_u32(dst);
-  const int sz = valid ? (int)sizeof(T) : 0;
-  if constexpr (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(sz) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // Shared-memory footprints, in elements of T.  Every group region starts with a
 // kHdr-element header (scalars broadcast between the group's warps).
 constexpr int kHdr = 16;

@@ -145,3 +145,69 @@ def test_gbmm_full_size(bm, gpu, orc, dt):
         if r > 32:
             mask[r, n - (r - 32):] = False
     assert np.array_equal(got[mask], ref[mask])
+
+
+def _dev_band_ld(bm, data_np, m, l, u, device, lda):
+    rows, n = data_np.shape
+    dt = torch.float64 if data_np.dtype == np.float64 else torch.float32
+    d = bm.band_storage(rows, n, dt, device, lda=lda, fill=float("nan"))
+    d.copy_(torch.from_numpy(np.ascontiguousarray(data_np)))
+    return bm.BandedMatrix(d, m, l, u)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,nu,m,Al,Au,Bl,Bu,pad,alpha", [
+    (3000, 3000, 3000, 16, 16, 16, 16, 0, 1.0),    # 33 x 33 bands, exact size class
+    (3000, 3000, 3000, 4, 3, 4, 3, 0, 1.0),        # the (4,3) x (4,3) product
+    (2500, 2600, 2700, 7, 1, 0, 5, 3, 0.75),       # non-square, padded leading dims
+    (2900, 2900, 2900, 10, 5, 2, 3, 1, -1.5),      # NA = 16, NB = 6 in the 17 class
+    (2100, 2100, 2100, 0, 0, 20, 12, 0, 2.0),      # diagonal times a 33-row band
+    (2100, 2100, 2100, 31, 1, 0, 0, 2, 1.0),       # 33-row band times a diagonal
+    (1500, 1500, 1500, 8, 8, 8, 8, 0, 0.5),        # 17 x 17, exact
+])
+def test_gbmm_interior_tiles_bitexact(bm, gpu, orc, dt, n, nu, m, Al, Au, Bl, Bu, pad, alpha):
+    """Shapes with interior column tiles (the register-blocked path, beta == 0): every
+    in-matrix entry equals the oracle's _gbmm! bit for bit, the edge columns included."""
+    rng = np.random.default_rng(n + Al * 7 + Bu)
+    A = rng.uniform(-1, 1, (Al + Au + 1, nu)).astype(dt)
+    B = rng.uniform(-1, 1, (Bl + Bu + 1, m)).astype(dt)
+    A[rng.integers(0, Al + Au + 1, 50), rng.integers(0, nu, 50)] = 0.0
+    Ad = _dev_band_ld(bm, A, n, Al, Au, gpu, Al + Au + 1 + pad)
+    Bd = _dev_band_ld(bm, B, nu, Bl, Bu, gpu, Bl + Bu + 1 + pad)
+    l, u = Al + Bl, Au + Bu
+    Cd = _dev_band_ld(bm, np.zeros((l + u + 1, m), dtype=dt), n, l, u, gpu, l + u + 1 + pad)
+    Cd.data.fill_(float("nan"))
+    bm.banded_mul_(Cd, Ad, Bd, alpha, 0.0)
+    ref = orc.gbmm_percol(n, nu, m, Al, Au, Bl, Bu, alpha, A, B, 0.0, np.zeros((l + u + 1, m), dtype=dt, order="F"))
+    got = Cd.data.cpu().numpy()
+    assert np.array_equal(in_matrix(orc, got, n, l, u), in_matrix(orc, ref, n, l, u))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_gbmm_interior_wide_c(bm, gpu, orc, dt):
+    """C with extra bands on both sides (beta == 0): product rows exact, extra in-matrix
+    rows zero, out-of-matrix storage untouched."""
+    rng = np.random.default_rng(21)
+    n = 2600
+    Al, Au, Bl, Bu = 5, 6, 3, 2
+    Cl, Cu = Al + Bl + 4, Au + Bu + 3
+    A = rng.standard_normal((Al + Au + 1, n)).astype(dt)
+    B = rng.standard_normal((Bl + Bu + 1, n)).astype(dt)
+    Cd = bm.BandedMatrix(bm.band_storage(Cl + Cu + 1, n, torch.float64 if dt == np.float64 else torch.float32,
+                                         gpu, fill=7.0), n, Cl, Cu)
+    bm.banded_mul_(Cd, dev_band(bm, A, n, Al, Au, gpu), dev_band(bm, B, n, Bl, Bu, gpu), 1.0, 0.0)
+    got = Cd.data.cpu().numpy()
+    ref = orc.gbmm_percol(n, n, n, Al, Au, Bl, Bu, 1.0, A, B, 0.0,
+                          np.zeros((Al + Bl + Au + Bu + 1, n), dtype=dt, order="F"))
+    sh = Cu - (Au + Bu)
+    mask = in_matrix(orc, np.ones((Al + Bl + Au + Bu + 1, n)), n, Al + Bl, Au + Bu) != 0
+    dref = in_matrix(orc, ref, n, Al + Bl, Au + Bu)
+    dgot = in_matrix(orc, got, n, Cl, Cu)
+    assert np.array_equal(dgot[mask], dref[mask])
+    assert (dgot[~mask] == 0).all()
+    for r in range(Cl + Cu + 1):  # storage slots outside the matrix keep their fill
+        for j in (0, 1, n - 2, n - 1):
+            k = j + r - Cu
+            if k < 0 or k >= n:
+                assert got[r, j] == 7.0, (r, j)
+    assert sh == 3
