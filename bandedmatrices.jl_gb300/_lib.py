@@ -25,11 +25,13 @@ F = ctypes.c_float
 C = ctypes.c_char
 I = ctypes.c_int
 
-# name -> argtypes (every entry point returns int)
+# name -> argtypes (every entry point returns int, except bm_last_error and bm_launch_count)
 SIGNATURES: dict[str, list] = {
     "bm_version": [],
     "bm_last_error": [],
     "bm_device_status": [P, I, P],
+    "bm_launch_count": [],
+    "bm_probe_fma_rate": [I, P, P],
     "bm_dgbmv": [C, i64, i64, i64, i64, D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmv": [C, i64, i64, i64, i64, F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm": [i64] * 9 + [D, P, i64, P, i64, D, P, i64, P],
@@ -78,7 +80,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
     for name, argt in SIGNATURES.items():
         fn = getattr(L, name)
         fn.argtypes = argt
-        fn.restype = ctypes.c_char_p if name == "bm_last_error" else ctypes.c_int
+        fn.restype = (ctypes.c_char_p if name == "bm_last_error"
+                      else ctypes.c_ulonglong if name == "bm_launch_count" else ctypes.c_int)
     _lib = L
     return L
 

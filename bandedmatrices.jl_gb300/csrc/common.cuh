@@ -30,7 +30,8 @@ inline int cuda_status(cudaError_t e, const char* where) {
   return BM_ERR_CUDA;
 }
 
-inline int launch_status(const char* where) { return cuda_status(cudaGetLastError(), where); }
+// Checks the launch just enqueued and counts it (bm_launch_count).
+int launch_status(const char* where);
 
 inline i64 ceil_div(i64 a, i64 b) { return (a + b - 1) / b; }
 

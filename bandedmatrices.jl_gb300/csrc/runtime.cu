@@ -1,4 +1,5 @@
 // Host runtime of the library: error text, device properties, status word.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <map>
@@ -19,6 +20,12 @@ void set_error(const char* fmt, ...) {
 }
 
 static std::mutex g_mu;
+static std::atomic<unsigned long long> g_launches{0};
+
+int launch_status(const char* where) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cuda_status(cudaGetLastError(), where);
+}
 
 int num_sms() {
   static std::map<int, int> cache;
@@ -86,3 +93,6 @@ extern "C" int bm_device_status(int* status_out, int clear, bm_stream_t stream) 
   }
   return bm::cuda_status(cudaStreamSynchronize(s), "bm_device_status");
 }
+
+// Kernels this library has enqueued in the process (captured launches included).
+extern "C" unsigned long long bm_launch_count(void) { return bm::g_launches.load(std::memory_order_relaxed); }

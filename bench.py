@@ -43,6 +43,17 @@ def gbmv_bytes(n, l, u, s):
     return s * n * (l + u + 1 + 2)
 
 
+def gbmv_fmas(n, l, u):
+    """Multiply-adds of y = A*x for a square n x n band (every in-matrix entry once)."""
+    return n * (l + u + 1) - l * (l + 1) // 2 - u * (u + 1) // 2
+
+
+def gbmm_fmas(n, l, u):
+    """Multiply-adds of C = A*B for two square n x n (l,u) bands (interior count per column)."""
+    w = l + u + 1
+    return n * w * w
+
+
 def gbmm_bytes(n, l, u, s):
     # A and B (l+u+1)*n each, C (2l+2u+1)*n written
     return s * n * ((l + u + 1) * 2 + (2 * l + 2 * u + 1))
@@ -249,13 +260,16 @@ def run_gpu(args, rank, world):
     for _, fn, _ in calls:
         fn()  # first call: per-device set-up outside capture
     torch.cuda.synchronize()
+    lib = bm._lib.load()
     graphs = []
+    n_launch = 0  # library kernels per step, counted by the library itself
     for lab, fn, nb in calls:
         gr = torch.cuda.CUDAGraph()
+        c0 = lib.bm_launch_count()
         with torch.cuda.graph(gr):
             fn()
+        n_launch += lib.bm_launch_count() - c0
         graphs.append((lab, gr, nb))
-    n_launch = len(graphs)
     ev = {lab: [] for lab, _, _ in graphs}
 
     def step(record):
@@ -297,8 +311,17 @@ def run_gpu(args, rank, world):
         t_ms = statistics.mean(a.elapsed_time(b) for a, b in ev[lab])
         per_case.append({"case": lab, "GBps": nb / (t_ms / 1e3) / 1e9, "ms": t_ms, "bytes": nb})
     peak, peak_kind = _peaks()
+    fma_peak = {}
+    for eb in (8, 4):  # the FP64 / FP32 fma roofs, probed on this GPU
+        v = ctypes.c_double(0.0)
+        bm._lib.check(lib.bm_probe_fma_rate(eb, ctypes.byref(v), ctypes.c_void_p(stream.cuda_stream)), "probe")
+        fma_peak[eb] = v.value
     for c in per_case:
         c["frac_of_hbm"] = c["GBps"] / peak
+        lu = int(c["case"].split("_l")[1])
+        f = gbmv_fmas(N_GBMV, lu, lu) if c["case"].startswith("gbmv") else gbmm_fmas(N_GBMM, lu, lu)
+        c["fma_per_s"] = f / (c["ms"] / 1e3)
+        c["frac_of_fma_roof"] = c["fma_per_s"] / fma_peak[8 if "_f64_" in c["case"] else 4]
     dom = max(per_case, key=lambda c: c["ms"])
     traffic = _traffic(dom["case"])
 
@@ -316,10 +339,16 @@ def run_gpu(args, rank, world):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "kernel": dom["case"], "achieved": dom["GBps"], "peak": peak,
                          "unit": "GB/s", "frac": dom["GBps"] / peak, "traffic": traffic,
-                         "peak_source": f"{peak_kind} hbm_gbs"},
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         # the Float64 cases are bounded first by the FP64 pipe (probed fma rate)
+                         "compute_roof": {"unit": "fma/s", "achieved": dom["fma_per_s"],
+                                          "peak": fma_peak[8 if "_f64_" in dom["case"] else 4],
+                                          "frac": dom["frac_of_fma_roof"],
+                                          "peak_source": "probed (bm_probe_fma_rate)"}},
             "sweep": per_case,
             "e2e": e2e,
             "gpu_launches": n_launch * args.steps,
+            "fma_roofs": {"f64": fma_peak[8], "f32": fma_peak[4]},
             "clocks": clk.summary(),
         }
     return out
@@ -548,6 +577,82 @@ def run_pde(bm, dev, stream, G=96):
             "forward_ms": t_f, "adjoint_ms": t_b, "fd_rel_err": abs(fd - ad) / max(1.0, abs(fd))}
 
 
+def run_case(args):
+    """One named workload, repeated --reps times (for profiler captures); prints the
+    device time of each repetition.  Cases: gbmv_{f32,f64}_l{L}, gbmm_{f32,f64}_l{L},
+    batched_plain, batched_mixed, lu_single_l{L}, qr_l{L}."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+
+    bm = ge.package()
+    bm.load_library()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    name = args.case
+    parts = name.split("_")
+    dt = torch.float32 if "f32" in parts else torch.float64
+    lu = int(name.split("_l")[-1]) if "_l" in name else 0
+    if parts[0] == "gbmv":
+        n = args.n or N_GBMV
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
+        A.data.uniform_(-1.0, 1.0, generator=g)
+        x = torch.randn(n, dtype=dt, device=dev, generator=g)
+        y = torch.empty(n, dtype=dt, device=dev)
+        fn = lambda: bm.gbmv("N", 1.0, A, x, 0.0, y)
+    elif parts[0] == "gbmm":
+        n = args.n or N_GBMM
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
+        B = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
+        A.data.uniform_(-1.0, 1.0, generator=g)
+        B.data.uniform_(-1.0, 1.0, generator=g)
+        C = bm.BandedMatrix(bm.band_storage(4 * lu + 1, n, dt, dev), n, 2 * lu, 2 * lu)
+        fn = lambda: bm.banded_mul_(C, A, B, 1.0, 0.0)
+    elif parts[0] == "batched":
+        n, kl, ku, nrhs = batched_config(n_sys=args.systems or 4096)
+        batch = bm.BandedBatch(n, kl, ku, nrhs, torch.float64, dev)
+        for s in range(batch.count):
+            mb = batch.matrix_band(s)
+            mb.normal_(generator=g)
+            mb[int(ku[s])] += 2.0 * (kl[s] + ku[s])
+            batch.rhs(s).normal_(generator=g)
+        AB0, B0 = batch.AB.clone(), batch.B.clone()
+        if parts[1] == "plain":
+            def fn():
+                batch.AB.copy_(AB0)
+                batch.B.copy_(B0)
+                batch.factor_solve()
+        else:
+            fn = lambda: batch.solve_mixed(1e-10, 30)
+    elif parts[0] == "lu":
+        n = args.n or 10000
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
+        A.data.normal_(generator=g)
+        A.data[lu] += 2.0 * lu + 1.0
+        b = torch.randn(n, dtype=dt, device=dev, generator=g)
+        fn = lambda: A.solve(b)
+    elif parts[0] == "qr":
+        n = args.n or (1 << 18)
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
+        A.data.normal_(generator=g)
+        fn = lambda: bm.qr(A)
+    else:
+        raise SystemExit(f"unknown case {name}")
+    fn()
+    torch.cuda.synchronize()
+    for r in range(args.reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        print(f"{name} rep {r}: {e0.elapsed_time(e1):.3f} ms", flush=True)
+    del np
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -556,7 +661,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-only", action="store_true", help="time only the gbmv/gbmm sweep")
+    ap.add_argument("--case", default=None, help="run one named workload (profiler captures)")
+    ap.add_argument("--n", type=int, default=0, help="--case: matrix order")
+    ap.add_argument("--reps", type=int, default=3, help="--case: repetitions")
+    ap.add_argument("--systems", type=int, default=0, help="--case batched_*: number of systems")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
 

@@ -46,6 +46,15 @@ const char *bm_last_error(void);
  * in-kernel wait expired.  `clear` resets it.  Synchronises the stream. */
 int bm_device_status(int *status_out, int clear, bm_stream_t stream);
 
+/* Diagnostics (no reference counterpart).  Kernels this library has enqueued in
+ * the process, captured launches included. */
+unsigned long long bm_launch_count(void);
+
+/* The fma rate (fmas per second) the current GPU sustains for elements of
+ * elem_bytes = 8 (Float64) or 4 (Float32): the compute roof of the kernels the
+ * FP64 pipe bounds.  Runs a short probe kernel; synchronises the stream. */
+int bm_probe_fma_rate(int elem_bytes, double *fma_per_s, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ gbmv
  * y <- alpha*op(A)*x + beta*y, op = 'N' | 'T' (| 'C' = 'T' for real types).
  * Replaces the dgbmv_/sgbmv_ ccall of src/blas.jl:16-28 and the stdlib
