@@ -4,11 +4,11 @@
 // BLAS.gbmv! from banded_gbmv!, src/generic/matmul.jl:21-23).
 //
 // Fast path (incx = incy = 1, 16-byte aligned A and x): a persistent kernel,
-// one CTA per SM.  Work is cut into tiles of consecutive outputs; for each tile
-// thread 0 streams the band columns the tile touches, and the x window, from
-// HBM into a shared-memory ring of `stages` buffers with 1-D TMA bulk copies
-// (cp.async.bulk, completion on an mbarrier), while all threads reduce the
-// previous buffer.  Each output element is owned by one thread and accumulated
+// one or two CTAs per SM.  Work is cut into tiles of consecutive outputs; for each
+// tile a producer warp streams the band columns the tile touches, and the x window,
+// from HBM into a shared-memory ring of `stages` buffers with 1-D TMA bulk copies
+// (cp.async.bulk, completion on an mbarrier), while 15 consumer warps reduce earlier
+// buffers and hand each one back through an mbarrier of its own.  Each output element is owned by one thread and accumulated
 // in the reference-BLAS order (see below), so the result is deterministic and
 // equal, bit for bit, to reference dgbmv compiled with fused multiply-adds.
 //
@@ -83,86 +83,131 @@ __device__ __forceinline__ void tile_ranges(const GbmvParams<T>& p, i64 t, i64& 
   }
 }
 
+// Ring protocol (no block-wide barrier in the loop).  Warp 0 is the producer, warps
+// 1..15 the consumers.  Slot s has three mbarriers:
+//   full[s]  (2 arrivals + tx bytes): the producer's arrive.expect_tx before the bulk
+//            copies, and its arrive after it stored the ragged tails;
+//   ready[s] (1 arrival, alpha != 1 in 'N' only): the producer scaled x by alpha;
+//   empty[s] (15 arrivals): each consumer warp is done reading the slot.
+// Every wait is bounded (kSpinLimit polls); on expiry the status word gets
+// BM_STATUS_TIMEOUT, the consumers stop and the producer waits (bounded) for the
+// copies still in flight before the CTA exits.
+constexpr int kGbmvThreads = 512;
+constexpr int kGbmvConsumers = kGbmvThreads / 32 - 1;
+
 template <typename T, bool TRANS>
-__device__ __forceinline__ void issue_tile(const GbmvParams<T>& p, unsigned char* slots, uint64_t* bars, i64 k) {
+__device__ __forceinline__ bool produce_tile(const GbmvParams<T>& p, unsigned char* slots, uint64_t* full,
+                                             uint64_t* ready, i64 k, int lane) {
   const i64 t = (i64)blockIdx.x + k * (i64)gridDim.x;
-  if (t >= p.ntiles) return;
   const int s = (int)(k % p.stages);
   i64 o0, o1, c0, c1, x0, x1;
   tile_ranges<T, TRANS>(p, t, o0, o1, c0, c1, x0, x1);
-  Region<T> ra = make_region<T>(c0 * p.lda, c1 * p.lda);
-  Region<T> rx = make_region<T>(x0, x1);
-  const uint32_t ba = (uint32_t)((ra.ge - ra.gs) * (i64)sizeof(T));
-  const uint32_t bx = (uint32_t)((rx.ge - rx.gs) * (i64)sizeof(T));
-  unsigned char* slot = slots + (size_t)s * p.stage_bytes;
-  fence_proxy_async_smem();
-  mbar_arrive_expect_tx(&bars[s], ba + bx);
-  if (ba) bulk_g2s(slot, p.A + ra.gs, ba, &bars[s]);
-  if (bx) bulk_g2s(slot + p.xoff, p.x + rx.gs, bx, &bars[s]);
+  const Region<T> ra = make_region<T>(c0 * p.lda, c1 * p.lda);
+  const Region<T> rx = make_region<T>(x0, x1);
+  T* sa = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes);
+  T* sx = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes + p.xoff);
+  if (lane == 0) {
+    const uint32_t ba = (uint32_t)((ra.ge - ra.gs) * (i64)sizeof(T));
+    const uint32_t bx = (uint32_t)((rx.ge - rx.gs) * (i64)sizeof(T));
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&full[s], ba + bx);
+    if (ba) bulk_g2s(sa, p.A + ra.gs, ba, &full[s]);
+    if (bx) bulk_g2s(sx, p.x + rx.gs, bx, &full[s]);
+  }
+  // ragged tails (< 16 bytes) the bulk copies leave out
+  const int na = (int)(ra.end - ra.ge), nx = (int)(rx.end - rx.ge);
+  if (lane < na) sa[ra.ge - ra.gs + lane] = p.A[ra.ge + lane];
+  else if (lane >= 16 && lane - 16 < nx) sx[rx.ge - rx.gs + lane - 16] = p.x[rx.ge + lane - 16];
+  __syncwarp();
+  if (lane == 0) mbar_arrive(&full[s]);
+  if (!TRANS && p.alpha != T(1)) {  // x <- alpha*x once per slot (the column dgbmv's temp)
+    const bool ok = mbar_wait(&full[s], (uint32_t)((k / p.stages) & 1));
+    if (!__all_sync(0xffffffffu, ok)) return false;
+    for (i64 e = x0 + lane; e < x1; e += 32) sx[e - rx.gs] = p.alpha * sx[e - rx.gs];
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&ready[s]);
+  }
+  return true;
 }
 
 template <typename T, bool TRANS>
-__global__ void __launch_bounds__(512) gbmv_tma_kernel(const GbmvParams<T> p) {
+__global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams<T> p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
-  unsigned char* slots = smem + 128;
-
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* ready = full + 8;
+  uint64_t* empty = full + 16;
+  unsigned char* slots = smem + 256;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < p.stages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < p.stages; ++s) {
+      mbar_init(&full[s], 2);
+      mbar_init(&ready[s], 1);
+      mbar_init(&empty[s], kGbmvConsumers);
+    }
     fence_mbar_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int k = 0; k < p.stages; ++k) issue_tile<T, TRANS>(p, slots, bars, k);
+  const i64 my_tiles = p.ntiles > blockIdx.x ? (p.ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
-  i64 k = 0;
-  bool failed = false;
-  for (;; ++k) {
+  if (warp == 0) {  // ---------------------------------------------------------- producer
+    bool ok = true;
+    i64 k = 0;
+    for (; k < my_tiles; ++k) {
+      if (k >= p.stages) {  // the consumers released tile k - stages from this slot
+        const bool w = mbar_wait(&empty[k % p.stages], (uint32_t)((k / p.stages - 1) & 1));
+        ok = __all_sync(0xffffffffu, w);
+        if (!ok) break;
+      }
+      if (!produce_tile<T, TRANS>(p, slots, full, ready, k, lane)) {
+        ok = false;
+        ++k;
+        break;
+      }
+    }
+    if (!ok) {
+      if (lane == 0) record_status(p.status, BM_STATUS_TIMEOUT);
+    }
+    // let every copy this CTA issued land before it exits
+    for (i64 kk = std::max<i64>((i64)0, k - p.stages); kk < k; ++kk)
+      (void)mbar_wait(&full[kk % p.stages], (uint32_t)((kk / p.stages) & 1));
+    return;
+  }
+
+  // ------------------------------------------------------------------------ consumers
+  const int ct = threadIdx.x - 32, bd = kGbmvThreads - 32;
+  for (i64 k = 0; k < my_tiles; ++k) {
     const i64 t = (i64)blockIdx.x + k * (i64)gridDim.x;
-    if (t >= p.ntiles) break;
     const int s = (int)(k % p.stages);
     const uint32_t phase = (uint32_t)((k / p.stages) & 1);
-    const bool ok = mbar_wait(&bars[s], phase);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
+    bool ok = mbar_wait(&full[s], phase);
+    if (ok && !TRANS && p.alpha != T(1)) ok = mbar_wait(&ready[s], phase);
+    if (!__all_sync(0xffffffffu, ok)) {
+      if (lane == 0) record_status(p.status, BM_STATUS_TIMEOUT);
+      return;
     }
     i64 o0, o1, c0, c1, x0, x1;
     tile_ranges<T, TRANS>(p, t, o0, o1, c0, c1, x0, x1);
     const Region<T> ra = make_region<T>(c0 * p.lda, c1 * p.lda);
     const Region<T> rx = make_region<T>(x0, x1);
-    T* sa = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes);
-    T* sx = reinterpret_cast<T*>(slots + (size_t)s * p.stage_bytes + p.xoff);
-    // Ragged tails (< 16 bytes) that the bulk copies left out.
-    {
-      const int na = (int)(ra.end - ra.ge), nx = (int)(rx.end - rx.ge);
-      const int tid = threadIdx.x;
-      if (tid < na) sa[ra.ge - ra.gs + tid] = p.A[ra.ge + tid];
-      else if (tid >= 32 && tid - 32 < nx) sx[rx.ge - rx.gs + tid - 32] = p.x[rx.ge + tid - 32];
-    }
-    if (!TRANS && p.alpha != T(1)) {
-      __syncthreads();
-      for (i64 e = x0 + threadIdx.x; e < x1; e += blockDim.x) sx[e - rx.gs] = p.alpha * sx[e - rx.gs];
-    }
-    __syncthreads();
+    const T* sa = reinterpret_cast<const T*>(slots + (size_t)s * p.stage_bytes);
+    const T* sx = reinterpret_cast<const T*>(slots + (size_t)s * p.stage_bytes + p.xoff);
 
     // Tile-local 32-bit indexing.  For 'N', outputs are rows i and A's columns are
     // local to c0; for 'T', outputs are columns j and x's rows are local to x0.
     const int nout = (int)(o1 - o0);
     const int lda = (int)p.lda, kl = (int)p.kl, ku = (int)p.ku, kb = kl + ku + 1;
-    const int bd = blockDim.x;
     if (!TRANS) {
       const int abase = (int)(c0 * p.lda - ra.gs) + ku;  // + jj*(lda-1) + li
       const int xbase = (int)(c0 - rx.gs);               // + jj
       const i64 nmax = p.n - 1 - c0;                     // last local column
       const int off = (int)(o0 - c0);                    // local index of row o0
-      for (int t = threadIdx.x; t < nout; t += 2 * bd) {
-        const int t2 = t + bd;
-        const int li = off + t, li2 = off + t2;
+      for (int tt = ct; tt < nout; tt += 2 * bd) {
+        const int t2 = tt + bd;
+        const int li = off + tt, li2 = off + t2;
         const bool two = t2 < nout;
-        const bool full1 = (o0 + t - kl >= 0) && (li + ku <= nmax);
+        const bool full1 = (o0 + tt - kl >= 0) && (li + ku <= nmax);
         const bool full2 = two && (o0 + t2 - kl >= 0) && (li2 + ku <= nmax);
-        T acc1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t];
+        T acc1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + tt];
         T acc2 = (two && p.beta != T(0)) ? p.beta * p.y[o0 + t2] : T(0);
         if (full1 && full2) {
           // two independent chains over all kb terms
@@ -192,21 +237,21 @@ __global__ void __launch_bounds__(512) gbmv_tma_kernel(const GbmvParams<T> p) {
             }
           }
         }
-        p.y[o0 + t] = acc1;
+        p.y[o0 + tt] = acc1;
         if (two) p.y[o0 + t2] = acc2;
       }
     } else {
       const int abase = (int)(o0 * p.lda - ra.gs) + ku;  // + lj*lda + (li - lj) with li local to o0
       const int xbase = (int)(o0 - rx.gs);               // + li
       const i64 mmax = p.m - 1 - o0;
-      for (int t = threadIdx.x; t < nout; t += 2 * bd) {
-        const int t2 = t + bd;
+      for (int tt = ct; tt < nout; tt += 2 * bd) {
+        const int t2 = tt + bd;
         const bool two = t2 < nout;
-        const bool full1 = (o0 + t - ku >= 0) && (t + kl <= mmax);
+        const bool full1 = (o0 + tt - ku >= 0) && (tt + kl <= mmax);
         const bool full2 = two && (o0 + t2 - ku >= 0) && (t2 + kl <= mmax);
         T acc1 = T(0), acc2 = T(0);
         if (full1 && full2) {
-          int ia = abase + t * lda - ku, ix = xbase + t - ku;
+          int ia = abase + tt * lda - ku, ix = xbase + tt - ku;
           int ia2 = ia + bd * lda, ix2 = ix + bd;
 #pragma unroll 4
           for (int q = 0; q < kb; ++q) {
@@ -216,8 +261,8 @@ __global__ void __launch_bounds__(512) gbmv_tma_kernel(const GbmvParams<T> p) {
           }
         } else {
           {
-            const int ilo = (int)max((i64)(t - ku), -o0), ihi = (int)min((i64)(t + kl), mmax);
-            int ia = abase + t * lda + ilo - t, ix = xbase + ilo;
+            const int ilo = (int)max((i64)(tt - ku), -o0), ihi = (int)min((i64)(tt + kl), mmax);
+            int ia = abase + tt * lda + ilo - tt, ix = xbase + ilo;
             for (int li = ilo; li <= ihi; ++li) {
               acc1 = fma(sa[ia], sx[ix], acc1);
               ++ia; ++ix;
@@ -232,27 +277,16 @@ __global__ void __launch_bounds__(512) gbmv_tma_kernel(const GbmvParams<T> p) {
             }
           }
         }
-        const T y1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t];
-        p.y[o0 + t] = fma(p.alpha, acc1, y1);
+        const T y1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + tt];
+        p.y[o0 + tt] = fma(p.alpha, acc1, y1);
         if (two) {
           const T y2 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t2];
           p.y[o0 + t2] = fma(p.alpha, acc2, y2);
         }
       }
     }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) issue_tile<T, TRANS>(p, slots, bars, k + p.stages);
-  }
-
-  if (failed) {
-    if (threadIdx.x == 0) record_status(p.status, BM_STATUS_TIMEOUT);
-    // Let copies that are still in flight land before the CTA exits.
-    for (i64 kk = k; kk < k + p.stages; ++kk) {
-      const i64 t = (i64)blockIdx.x + kk * (i64)gridDim.x;
-      if (t >= p.ntiles) break;
-      (void)mbar_wait(&bars[kk % p.stages], (uint32_t)((kk / p.stages) & 1));
-    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
@@ -310,7 +344,7 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   i64 tile = 0, budget = 220 * 1024;
   if (const char* env = getenv("BM_GBMV_CFG")) {
     int c = 0, st = 0, kb = 0;
-    if (sscanf(env, "%d,%d,%d", &c, &st, &kb) == 3 && c >= 1 && c <= 4 && st >= 2 && st <= 8 && kb >= 16 &&
+    if (sscanf(env, "%d,%d,%d", &c, &st, &kb) == 3 && c >= 1 && c <= 2 && st >= 2 && st <= 8 && kb >= 16 &&
         kb <= 224) {
       ctas = c;
       stages = st;
@@ -319,14 +353,15 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   }
   auto tile_for = [&](int st) {
     const i64 slot = budget / st;
-    const i64 cols = (slot - 384) / per_out;
+    const i64 cols = (slot - 512) / per_out;
     return notr ? cols - halo : cols - (halo * s + per_out - 1) / per_out;
   };
   if (!stages) {
-    // Measured on GB300 (n = 2^24 sweep): two large ring slots beat deeper rings of
-    // smaller tiles; two CTAs per SM pay off for narrow bands, one for wide ones.
-    stages = 2;
-    if (halo <= 16) {
+    // Measured on GB300 (n = 2^24, l = u in {1, 8, 32}, f32 and f64): for 'N' one CTA
+    // per SM with two large ring slots (three for tridiagonal bands) is best or within
+    // 4% of best; 'T' gains from two CTAs per SM when the band is narrow.
+    stages = (notr && halo <= 2) ? 3 : 2;
+    if (!notr && halo <= 16) {
       ctas = 2;
       budget = 110 * 1024;
     }
@@ -362,7 +397,7 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   p.xoff = (uint32_t)abytes;
   p.stage_bytes = (uint32_t)(abytes + xbytes);
   p.status = status_word();
-  const int smem = 128 + stages * (int)p.stage_bytes;
+  const int smem = 256 + stages * (int)p.stage_bytes;
   if (smem > 227 * 1024) {
     set_error("%s: internal tile selection exceeded shared memory (%d bytes)", name, smem);
     return BM_ERR_UNSUPPORTED;
@@ -372,9 +407,9 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   if (r) return r;
   const i64 grid = std::min<i64>(p.ntiles, (i64)nsm * ctas);
   if (notr)
-    gbmv_tma_kernel<T, false><<<(unsigned)grid, 512, smem, stream>>>(p);
+    gbmv_tma_kernel<T, false><<<(unsigned)grid, kGbmvThreads, smem, stream>>>(p);
   else
-    gbmv_tma_kernel<T, true><<<(unsigned)grid, 512, smem, stream>>>(p);
+    gbmv_tma_kernel<T, true><<<(unsigned)grid, kGbmvThreads, smem, stream>>>(p);
   return launch_status(name);
 }
 

@@ -32,7 +32,7 @@ static int probe(double* fma_per_s, cudaStream_t stream) {
   if constexpr (sizeof(T) == 8) r = cuda_status(cudaGetSymbolAddress((void**)&d_sink, g_sink64), "bm_probe_fma_rate");
   else r = cuda_status(cudaGetSymbolAddress((void**)&d_sink, g_sink32), "bm_probe_fma_rate");
   if (r) return r;
-  const int blocks = num_sms() * 8, threads = 256, iters = 1 << 14;
+  const int blocks = num_sms() * 8, threads = 256, iters = sizeof(T) == 8 ? (1 << 11) : (1 << 15);
   cudaEvent_t e0, e1;
   if ((r = cuda_status(cudaEventCreate(&e0), "bm_probe_fma_rate"))) return r;
   if ((r = cuda_status(cudaEventCreate(&e1), "bm_probe_fma_rate"))) {
