@@ -54,6 +54,9 @@ SIGNATURES: dict[str, list] = {
     "bm_dgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
     "bm_sgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
     "bm_dsgbsv_batched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, i64, i64, P],
+    "bm_dgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P],
+    "bm_sgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P],
+    "bm_dsgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, P],
 }
 
 # bm_gb_desc as a numpy structured dtype (9 x int64, C layout)

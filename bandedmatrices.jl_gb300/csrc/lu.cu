@@ -29,31 +29,53 @@ __global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, in
                     ldb, reinterpret_cast<T*>(smem_raw));
 }
 
-// Persistent batched factor + solve.  Each group (G = 1: each warp; G > 1: the CTA)
-// takes the next system from a device work queue (an atomic counter over `order`,
-// which lists systems from the most to the least expensive), factors it in place and
-// solves its right-hand sides.  Shared memory per group is sized for the widest band
-// of the batch.
+// Factor + solve of one system of a batch by a group of G warps.
 template <typename T, int G>
-__global__ void __launch_bounds__(G == 1 ? 128 : 32 * G) gbsv_batched_kernel(
-    i64 count, const bm_gb_desc* __restrict__ descs, const int32_t* __restrict__ order, T* AB, i64* ipiv, T* B,
-    i64* info, int32_t* counter, i64 group_elems) {
+__device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i64* ipiv, T* B, i64* info, T* smem) {
+  T* ab = AB + d.ab_offset;
+  i64* ip = ipiv + d.ipiv_offset;
+  const i64 r = gbtrf_group<T, kP, G>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
+  if (Grp<G>::tid() == 0) info[s] = r;
+  Grp<G>::sync();
+  if (r == 0) gbtrs_all<T, G>(false, d.n, (int)d.kl, (int)d.ku, d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem);
+  Grp<G>::sync();
+}
+
+// Persistent batched factor + solve with a two-part schedule.  `order` lists the
+// systems, wide ones first (most expensive first within each part).  Part 1: the
+// CTA (W warps) takes the next wide system from the work queue (an atomic counter
+// over `order`) and solves it as one group.  Part 2: once the queue reaches
+// order[n_wide], each warp takes narrow systems on its own, in a shared-memory slice
+// of narrow_elems elements.  Every system is factored in place and its right-hand
+// sides solved; info[s] receives its gbtrf info.
+template <typename T, int W>
+__global__ void __launch_bounds__(32 * W) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
+                                                             const int32_t* __restrict__ order, i64 n_wide, T* AB,
+                                                             i64* ipiv, T* B, i64* info, int32_t* counter,
+                                                             i64 narrow_elems) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
-  T* smem = reinterpret_cast<T*>(smem_raw) + grp * group_elems;
-  int* hdr = reinterpret_cast<int*>(smem);
+  T* base = reinterpret_cast<T*>(smem_raw);
+  int idx;
   for (;;) {
-    const int idx = next_item<G>(counter, hdr);
-    if (idx >= count) break;
+    idx = next_item<W>(counter, reinterpret_cast<int*>(base));
+    if (idx >= n_wide) break;
     const int s = order ? order[idx] : idx;
-    const bm_gb_desc d = descs[s];
-    T* ab = AB + d.ab_offset;
-    i64* ip = ipiv + d.ipiv_offset;
-    const i64 r = gbtrf_group<T, kP, G>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
-    if (Grp<G>::tid() == 0) info[s] = r;
-    Grp<G>::sync();
-    if (r == 0) gbtrs_all<T, G>(false, d.n, (int)d.kl, (int)d.ku, d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem);
-    Grp<G>::sync();
+    gbsv_system<T, W>(descs[s], s, AB, ipiv, B, info, base);
+    __syncthreads();
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* ws = base + w * narrow_elems;
+  int my = w == 0 ? idx : -1;  // the CTA's first narrow system goes to warp 0
+  for (;;) {
+    if (my < 0) {
+      int v = 0;
+      if (lane == 0) v = atomicAdd(counter, 1);
+      my = __shfl_sync(0xffffffffu, v, 0);
+    }
+    if (my >= count) break;
+    const int s = order ? order[my] : my;
+    gbsv_system<T, 1>(descs[s], s, AB, ipiv, B, info, ws);
+    my = -1;
   }
 }
 
@@ -77,7 +99,11 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
               (long long)ku);
     return BM_ERR_UNSUPPORTED;
   }
-  if (use_cta_group(kl, ku)) {
+  if (use_cta_group(kl, ku) && kl + ku + 1 > 128) {  // one thread per window column
+    int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T, 8>, (int)bytes), name);
+    if (r) return r;
+    gbtrf_one_kernel<T, 8><<<1, 256, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+  } else if (use_cta_group(kl, ku)) {
     int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T, 4>, (int)bytes), name);
     if (r) return r;
     gbtrf_one_kernel<T, 4><<<1, 128, (int)bytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
@@ -121,45 +147,78 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
   return launch_status(name);
 }
 
+// Shared memory of one group solving systems up to (kl, ku), 16-byte rounded, in T.
+template <typename T>
+static i64 group_elems(i64 kl, i64 ku) {
+  const i64 e = std::max(gbtrf_smem_elems<kP>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku));
+  return ((e * (i64)sizeof(T) + 15) / 16) * 16 / (i64)sizeof(T);
+}
+
+template <typename T, int W>
+static int gbsv_batched_launch(i64 count, const bm_gb_desc* descs, const int32_t* order, const bm_gb_schedule& sc,
+                               T* AB, i64* ipiv, T* B, i64* info, int32_t* counter, cudaStream_t stream,
+                               const char* name) {
+  const i64 we = sc.n_wide > 0 ? group_elems<T>(sc.wide_kl, sc.wide_ku) : 0;
+  const i64 ne = sc.n_wide < count ? group_elems<T>(sc.narrow_kl, sc.narrow_ku) : 0;
+  const i64 elems = std::max(std::max(we, W * ne), (i64)kHdr);
+  const i64 bytes = elems * (i64)sizeof(T);
+  if (bytes > 227 * 1024) {
+    set_error("%s: the schedule's shared memory (%lld bytes) exceeds the per-CTA limit", name, (long long)bytes);
+    return BM_ERR_UNSUPPORTED;
+  }
+  const void* kfn = (const void*)gbsv_batched_kernel<T, W>;
+  int r = cuda_status(ensure_smem(kfn, (int)bytes), name);
+  if (r) return r;
+  int per_sm = 0;
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gbsv_batched_kernel<T, W>, 32 * W, (int)bytes),
+                  name);
+  if (r) return r;
+  per_sm = std::max(per_sm, 1);
+  const i64 need = sc.n_wide + ceil_div(count - sc.n_wide, (i64)W);
+  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, std::max<i64>(need, 1));
+  r = cuda_status(cudaMemsetAsync(counter, 0, sizeof(int32_t), stream), name);
+  if (r) return r;
+  gbsv_batched_kernel<T, W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(count, descs, order, sc.n_wide, AB, ipiv,
+                                                                           B, info, counter, ne);
+  return launch_status(name);
+}
+
+template <typename T>
+static int gbsv_batched_sched_impl(i64 count, const bm_gb_desc* descs, const int32_t* order, const bm_gb_schedule* sc,
+                                   T* AB, i64* ipiv, T* B, i64* info, int32_t* counter, cudaStream_t stream,
+                                   const char* name) {
+  if (count < 0) return -1;
+  if (!descs && count) return -2;
+  if (!sc) return -4;
+  if (sc->n_wide < 0 || sc->n_wide > count || (sc->warps != 4 && sc->warps != 8) || sc->wide_kl < 0 ||
+      sc->wide_ku < 0 || sc->narrow_kl < 0 || sc->narrow_ku < 0)
+    return -4;
+  if (!counter) return -9;
+  if (count == 0) return BM_OK;
+  if (sc->warps == 8) return gbsv_batched_launch<T, 8>(count, descs, order, *sc, AB, ipiv, B, info, counter, stream, name);
+  return gbsv_batched_launch<T, 4>(count, descs, order, *sc, AB, ipiv, B, info, counter, stream, name);
+}
+
+// The schedule of the single-part entry points: every system wide (one CTA of 4 warps
+// each) when the widest window holds 512 entries or more, else every system narrow.
+inline bm_gb_schedule default_schedule(i64 count, i64 max_kl, i64 max_ku) {
+  bm_gb_schedule sc;
+  sc.n_wide = use_cta_group(max_kl, max_ku) ? count : 0;
+  sc.warps = 4;
+  sc.wide_kl = sc.narrow_kl = max_kl;
+  sc.wide_ku = sc.narrow_ku = max_ku;
+  return sc;
+}
+
 template <typename T>
 static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* order, T* AB, i64* ipiv, T* B,
                              i64* info, int32_t* counter, i64 max_kl, i64 max_ku, cudaStream_t stream,
                              const char* name) {
-  if (count < 0) return -1;
-  if (!descs && count) return -2;
   if (max_kl < 0) return -10;
   if (max_ku < 0) return -11;
-  if (!counter) return -9;
-  if (count == 0) return BM_OK;
-  const i64 welems = std::max(gbtrf_smem_elems<kP>((int)max_kl, (int)max_ku), gbtrs_smem_elems((int)max_kl, (int)max_ku));
-  const i64 wbytes = ((welems * (i64)sizeof(T) + 15) / 16) * 16;
-  const i64 welems_aligned = wbytes / (i64)sizeof(T);
-  if (wbytes > 227 * 1024) {
-    set_error("%s: widest band of the batch exceeds the per-warp window limit", name);
-    return BM_ERR_UNSUPPORTED;
-  }
-  const bool cta = use_cta_group(max_kl, max_ku);
-  // G = 1: as many warps per CTA as fit in ~100 KB (at most 4); G = 4: one system per CTA
-  const int wpc = cta ? 1 : (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
-  const int threads = cta ? 128 : 32 * wpc;
-  const int smem = (int)(wpc * wbytes);
-  const void* kfn = cta ? (const void*)gbsv_batched_kernel<T, 4> : (const void*)gbsv_batched_kernel<T, 1>;
-  int r = cuda_status(ensure_smem(kfn, smem), name);
-  if (r) return r;
-  int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem), name);
-  if (r) return r;
-  per_sm = std::max(per_sm, 1);
-  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(count, wpc));
-  r = cuda_status(cudaMemsetAsync(counter, 0, sizeof(int32_t), stream), name);
-  if (r) return r;
-  if (cta)
-    gbsv_batched_kernel<T, 4><<<(unsigned)grid, threads, smem, stream>>>(count, descs, order, AB, ipiv, B, info,
-                                                                          counter, welems_aligned);
-  else
-    gbsv_batched_kernel<T, 1><<<(unsigned)grid, threads, smem, stream>>>(count, descs, order, AB, ipiv, B, info,
-                                                                          counter, welems_aligned);
-  return launch_status(name);
+  const bm_gb_schedule sc = default_schedule(count, max_kl, max_ku);
+  const int r = gbsv_batched_sched_impl<T>(count, descs, order, &sc, AB, ipiv, B, info, counter, stream, name);
+  return r == -4 ? -10 : r;
 }
 
 // ---------------------------------------------------------------------------
@@ -277,6 +336,18 @@ extern "C" int bm_sgbtrs(char trans, int64_t n, int64_t kl, int64_t ku, int64_t 
                          const int64_t* ipiv, float* B, int64_t ldb, bm_stream_t stream) {
   return bm::gbtrs_impl<float>(trans, n, kl, ku, nrhs, AB, ldab, ipiv, B, ldb,
                                reinterpret_cast<cudaStream_t>(stream), "bm_sgbtrs");
+}
+extern "C" int bm_dgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, const int32_t* order,
+                                      const bm_gb_schedule* sched, double* AB, int64_t* ipiv, double* B, int64_t* info,
+                                      int32_t* counter, bm_stream_t stream) {
+  return bm::gbsv_batched_sched_impl<double>(count, descs, order, sched, AB, ipiv, B, info, counter,
+                                             reinterpret_cast<cudaStream_t>(stream), "bm_dgbsv_batched_sched");
+}
+extern "C" int bm_sgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, const int32_t* order,
+                                      const bm_gb_schedule* sched, float* AB, int64_t* ipiv, float* B, int64_t* info,
+                                      int32_t* counter, bm_stream_t stream) {
+  return bm::gbsv_batched_sched_impl<float>(count, descs, order, sched, AB, ipiv, B, info, counter,
+                                            reinterpret_cast<cudaStream_t>(stream), "bm_sgbsv_batched_sched");
 }
 extern "C" int bm_dgbsv_batched(int64_t count, const bm_gb_desc* descs, const int32_t* order, double* AB,
                                 int64_t* ipiv, double* B, int64_t* info, int32_t* counter, int64_t max_kl,

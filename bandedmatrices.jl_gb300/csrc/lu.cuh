@@ -109,7 +109,8 @@ __host__ __device__ inline int lu_rs(int kl) { return (kl + 1) | 1; }  // odd co
 template <int P>
 __host__ __device__ inline i64 gbtrf_smem_elems(int kl, int ku) {
   const int K = kl + ku + 1;
-  return kHdr + (i64)lu_rs(kl) * K + (i64)P * K;
+  // header + window + staging ring + the step's multipliers (kl+1)
+  return kHdr + (i64)lu_rs(kl) * K + (i64)P * K + (kl + 1);
 }
 
 constexpr int kChunk = 32;  // solve steps staged per chunk
@@ -146,10 +147,44 @@ __device__ __forceinline__ void grp_shift_up(T* X, int count, int d) {
   }
 }
 
+// a[r] = fma(l[r], nu, a[r]) for r < len; chunks of 8 with every load of a chunk
+// issued before its stores (a and l never overlap)
+template <typename T>
+__device__ __forceinline__ void rank1_run(T* a, const T* l, int len, T nu) {
+  constexpr int kU = 8;
+  int r = 0;
+  for (; r + kU <= len; r += kU) {
+    T lv[kU], av[kU];
+#pragma unroll
+    for (int q = 0; q < kU; ++q) {
+      lv[q] = l[r + q];
+      av[q] = a[r + q];
+    }
+#pragma unroll
+    for (int q = 0; q < kU; ++q) a[r + q] = fma(lv[q], nu, av[q]);
+  }
+  for (; r < len; ++r) a[r] = fma(l[r], nu, a[r]);
+}
+
 // --------------------------------------------------------------------- gbtrf
 // Factors the m x n band in ab (LAPACK gbtrf storage, ldab >= 2kl+ku+1) in place;
 // writes 1-based pivots to ipiv[0..min(m,n)) and returns LAPACK's info (to every
 // thread of the group).
+//
+// Step j works on the window W (logical rows 0..kl = matrix rows j..j+kl, logical
+// columns 0..kv = matrix columns j..j+kv).  Physical window column p is owned by
+// thread p mod NT for the whole factorization; a step is two group barriers:
+//   phase 1 (all threads, column 0 only): with the pivot row jp known, the multipliers
+//     l_r = (1/piv) * a_r (the swapped-in a_jp = old a_0) are written over column 0
+//     and stored as L(j+r, j); U(j,j) = piv and ipiv[j] are stored.  The column that
+//     left the window last step is cleared for its new role as column kv.
+//   phase 2 (each owner, its columns c = 1..kv): swap rows 0 and jp, store U(j, j+c),
+//     the update a_r = fma(l_r, -u_c, a_r) (skipped for u_c == 0), and the slide (the
+//     entering row's value into the slot row 0 leaves).  The owner of column 1 then
+//     finds the next pivot (idamax of the new column 0), so the search is off the
+//     critical path of the other columns.
+// Columns beyond LAPACK's ju hold u_c = 0 in both swapped rows (nothing has filled
+// them), so treating every column like dgbtf2 treats columns <= ju changes no bit.
 template <typename T, int P, int G>
 __device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab, i64* __restrict__ ipiv,
                            T* __restrict__ smem) {
@@ -159,6 +194,7 @@ __device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64
   int* hdr = reinterpret_cast<int*>(smem);
   T* W = smem + kHdr;
   T* S = W + (i64)RS * K;
+  T* Lm = S + (i64)P * K;  // multipliers of the step, by logical row (1..km)
   const i64 mn = min(m, n);
   i64 info = 0;
   if (mn <= 0) return 0;
@@ -183,135 +219,140 @@ __device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64
   for (int p = 0; p < P; ++p) issue_row((i64)kl + 1 + p);
   Grp<G>::sync();
 
-  int pr0 = 0, pc0 = 0;
-  i64 ju = 0;
-  for (i64 j = 0; j < mn; ++j) {
-    const int km = (int)min((i64)kl, m - 1 - j);
-    // ---- pivot (warp 0): first index of the largest |a| over logical rows 0..km of
-    // column 0.  |a| is compared through its IEEE bit pattern (monotone for |a| >= 0), so
-    // the search runs on the integer pipe: a per-lane scan, then redux.sync max/min.
+  // idamax over logical rows 0..km of physical column pc (logical row r at physical
+  // (rb + r) mod R), run by the warp that owns pc; the result is returned to that
+  // warp's lanes.  Narrow bands: one thread scans with the reference's compares;
+  // wider: lanes compare IEEE bit patterns and combine with redux.sync.
+  auto find_pivot = [&](int pc, int rb, int km) -> int {
+    const T* col = W + pc * RS;
     int jp = 0;
-    T piv = T(0), old0 = T(0);
-    if (wig == 0) {
+    if (kl <= 8) {
+      if (tid == pc % NT) {
+        T amax = fabs(col[rb]);
+        for (int r = 1; r <= km; ++r) {
+          int pr = rb + r;
+          pr = pr >= R ? pr - R : pr;
+          const T a = fabs(col[pr]);
+          if (a > amax) {
+            amax = a;
+            jp = r;
+          }
+        }
+      }
+      jp = __shfl_sync(0xffffffffu, jp, (pc % NT) & 31);
+    } else {
+      __syncwarp();
       unsigned long long key = 0ull;
       int idx = 0x7fffffff;
       for (int r = lane; r <= km; r += 32) {
-        int pr = pr0 + r;
+        int pr = rb + r;
         pr = pr >= R ? pr - R : pr;
-        const unsigned long long k = pivot_key(W[pr + pc0 * RS], r == 0);
+        const unsigned long long k = pivot_key(col[pr], r == 0);
         if (idx == 0x7fffffff || k > key) {
           key = k;
           idx = r;
         }
       }
       jp = warp_argmax_first(key, idx);
-      int pp = pr0 + jp;
-      pp = pp >= R ? pp - R : pp;
-      piv = W[pp + pc0 * RS];
-      old0 = W[pr0 + pc0 * RS];  // row j's entry, moves to row j+jp by the interchange
-      if (lane == 0) {
-        ipiv[j] = j + jp + 1;
-        if (G > 1) {
-          hdr[0] = jp;
-          smem[2] = piv;  // T slots 2, 3 lie past the two int slots of the header
-          smem[3] = old0;
-        }
-      }
     }
-    // every thread holds jp, piv and old0 before any thread overwrites column 0
-    Grp<G>::sync();
+    return jp;
+  };
+
+  int pr0 = 0, pc0 = 0;
+  int jp = 0;
+  {
+    const int km0 = (int)min((i64)kl, m - 1);
+    if (wig == (0 % NT) >> 5) jp = find_pivot(0, 0, km0);
     if (G > 1) {
+      if (tid == 0) hdr[0] = jp;
+      Grp<G>::sync();
       jp = hdr[0];
-      piv = smem[2];
-      old0 = smem[3];
     }
+  }
+  for (i64 j = 0; j < mn; ++j) {
+    const int km = (int)min((i64)kl, m - 1 - j);
+    const bool last = (j + 1 == mn);
     int prp = pr0 + jp;
     prp = prp >= R ? prp - R : prp;
+    T* col0 = W + pc0 * RS;
+    const T piv = col0[prp];
     const bool nonsingular = is_nonzero(piv);
-    int nc = 0;
-    if (nonsingular) {
-      ju = max(ju, min(j + ku + jp, n - 1));
-      nc = (int)(ju - j);
-      // ---- interchange in column 0 and scaling by the reciprocal of the pivot (dscal)
-      if (km > 0) {
-        const T rcp = T(1) / piv;
-        for (int r = 1 + tid; r <= km; r += NT) {
-          int pr = pr0 + r;
-          pr = pr >= R ? pr - R : pr;
-          const T v = (r == jp) ? old0 : W[pr + pc0 * RS];
-          W[pr + pc0 * RS] = rcp * v;
-        }
-      } else if (jp != 0 && tid == 0) {
-        W[prp + pc0 * RS] = old0;
-      }
-      if (tid == 0) W[pr0 + pc0 * RS] = piv;
-      Grp<G>::sync();
-      // ---- per column c = 1..nc (one owner thread): interchange rows 0 and jp, then the
-      // rank-1 update a <- fma(l_r, -u_c, a) (dger, skipping u_c == 0).  Rows go in chunks
-      // of kU so that a chunk's shared-memory loads are in flight before its stores.
-      constexpr int kU = 8;
-      const T* col0 = W + pc0 * RS;
-      for (int c = 1 + tid; c <= nc; c += NT) {
-        int pc = pc0 + c;
-        pc = pc >= K ? pc - K : pc;
-        T* colc = W + pc * RS;
-        T uc = colc[pr0];
-        if (jp != 0) {
-          const T t = colc[prp];
-          colc[prp] = uc;
-          colc[pr0] = t;
-          uc = t;
-        }
-        if (km > 0 && is_nonzero(uc)) {
-          int pr = pr0;
-          for (int r0 = 1; r0 <= km; r0 += kU) {
-            T mv[kU], av[kU];
-            int pq[kU];
-#pragma unroll
-            for (int q = 0; q < kU; ++q) {
-              pr = pr + 1 == R ? 0 : pr + 1;
-              pq[q] = pr;
-              if (r0 + q <= km) {
-                mv[q] = col0[pr];
-                av[q] = colc[pr];
-              }
-            }
-#pragma unroll
-            for (int q = 0; q < kU; ++q)
-              if (r0 + q <= km) colc[pq[q]] = fma(mv[q], -uc, av[q]);
-          }
-        }
-      }
-    } else if (info == 0) {
-      info = j + 1;
+    // ---- phase 1: column 0 (multipliers into Lm, L and U(j,j) stores; column 0 itself
+    // is only read), and clear the column that left the window at the previous step
+    // (physical pc0-1, now logical column kv)
+    if (tid == 0) {
+      ipiv[j] = j + jp + 1;
+      ab[kv + j * ldab] = piv;
     }
-    const bool last = (j + 1 == mn);
+    if (km > 0) {
+      const T old0 = col0[pr0];
+      const T rcp = nonsingular ? T(1) / piv : T(0);
+      for (int r = 1 + tid; r <= km; r += NT) {
+        int pr = pr0 + r;
+        pr = pr >= R ? pr - R : pr;
+        T v = (nonsingular && r == jp) ? old0 : col0[pr];
+        if (nonsingular) v = rcp * v;
+        Lm[r] = v;
+        ab[(kv + r) + j * ldab] = v;
+      }
+    }
+    if (!nonsingular && info == 0) info = j + 1;
+    if (j > 0) {
+      int pcl = pc0 - 1;
+      pcl = pcl < 0 ? pcl + K : pcl;
+      const int prl = pr0 == 0 ? R - 1 : pr0 - 1;  // holds the row that entered last step
+      for (int r = tid; r < R; r += NT)
+        if (r != prl) W[r + pcl * RS] = T(0);
+    }
     if (!last) cp_async_wait<P - 1>();
     Grp<G>::sync();
-    // ---- write-back and slide, fused: the thread owning logical column c stores row j's
-    // entry (U(j, j+c)) and puts the entering row's value for that physical column in its
-    // place (column c becomes logical c-1; column 0 becomes logical kv, the new column);
-    // the thread owning row r of column 0 stores L(j+r, j) and zeroes the slot (fill-in).
+    // ---- phase 2: every other column, by its owner
     const i64 inew = j + 1 + kl;
     const T* st = S + (int)(inew & (P - 1)) * K;
     const int ncw = (int)min((i64)kv, n - 1 - j);
-    for (int c = tid; c < K; c += NT) {
-      int pc = pc0 + c;
-      pc = pc >= K ? pc - K : pc;
-      if (c <= ncw) ab[(kv - c) + (j + c) * ldab] = W[pr0 + pc * RS];
-      if (!last) W[pr0 + pc * RS] = st[c == 0 ? kv : c - 1];
-    }
-    for (int r = 1 + tid; r <= kl; r += NT) {
-      int pr = pr0 + r;
-      pr = pr >= R ? pr - R : pr;
-      if (r <= km) ab[(kv + r) + j * ldab] = W[pr + pc0 * RS];
-      W[pr + pc0 * RS] = T(0);
+    int p1 = pc0 + 1;
+    p1 = p1 >= K ? p1 - K : p1;
+    for (int pcc = tid; pcc < K; pcc += NT) {
+      if (pcc == pc0) {
+        if (!last) col0[pr0] = st[kv];  // the new column kv's entry in the entering row
+        continue;
+      }
+      const int c = pcc >= pc0 ? pcc - pc0 : pcc - pc0 + K;
+      T* colc = W + pcc * RS;
+      T uc = colc[pr0];
+      if (nonsingular && jp != 0) {
+        const T t = colc[prp];
+        colc[prp] = uc;
+        uc = t;
+      }
+      if (c <= ncw) ab[(kv - c) + (j + c) * ldab] = uc;
+      if (nonsingular && km > 0 && is_nonzero(uc)) {
+        // logical rows 1..km are physical rows pr0+1.. (first segment) and then 0..
+        // (after the wrap): two runs with unit stride in both colc and Lm
+        const int s1 = min(km, R - 1 - pr0);
+        rank1_run<T>(colc + pr0 + 1, Lm + 1, s1, -uc);
+        rank1_run<T>(colc, Lm + 1 + s1, km - s1, -uc);
+      }
+      if (!last) colc[pr0] = st[c - 1];  // slide: the entering row takes row 0's slot
     }
     if (last) break;
+    // ---- next pivot, by the warp owning the next column 0 (physical p1)
+    {
+      const int pr1 = pr0 + 1 == R ? 0 : pr0 + 1;
+      const int km1 = (int)min((i64)kl, m - 2 - j);
+      int jn = 0;
+      if (wig == (p1 % NT) >> 5) jn = find_pivot(p1, pr1, km1);
+      if (G > 1) {
+        if (tid == p1 % NT) hdr[0] = jn;
+      } else {
+        jp = jn;
+      }
+    }
     Grp<G>::sync();
+    if (G > 1) jp = hdr[0];
     issue_row(inew + P);
     pr0 = pr0 + 1 == R ? 0 : pr0 + 1;
-    pc0 = pc0 + 1 == K ? 0 : pc0 + 1;
+    pc0 = p1;
   }
   cp_async_wait<0>();
   Grp<G>::sync();

@@ -123,20 +123,14 @@ struct MixedParams {
   i64 group_elems;   // shared-memory floats per group
 };
 
+// One system of the batch (index s) by a group of G warps in `smem`.
 template <int G>
-__global__ void __launch_bounds__(G == 1 ? 128 : 32 * G) dsgbsv_batched_kernel(const MixedParams p) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
   constexpr int NT = Grp<G>::NT;
-  const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
   const int tid = Grp<G>::tid(), wig = tid >> 5;
-  float* smem = reinterpret_cast<float*>(smem_raw) + grp * p.group_elems;
-  int* hdr = reinterpret_cast<int*>(smem);
   double* red = reinterpret_cast<double*>(smem + kHdr);  // reduction scratch (between phases)
   auto sync = [] { Grp<G>::sync(); };
-  for (;;) {
-    const int idx = next_item<G>(p.counter, hdr);
-    if (idx >= p.count) break;
-    const int s = p.order ? p.order[idx] : idx;
+  {
     const bm_gb_desc d = p.descs[s];
     const int kl = (int)d.kl, ku = (int)d.ku;
     const i64 n = d.n, ldab = d.ldab;
@@ -231,50 +225,86 @@ __global__ void __launch_bounds__(G == 1 ? 128 : 32 * G) dsgbsv_batched_kernel(c
   }
 }
 
-static int dsgbsv_batched_impl(const MixedParams& p0, i64 max_kl, i64 max_ku, cudaStream_t stream,
-                               const char* name) {
-  MixedParams p = p0;
+// Two-part schedule, as gbsv_batched_kernel: wide systems (order[0..n_wide)) one per
+// CTA of W warps, then narrow systems one per warp in group_elems-float slices.
+template <int W>
+__global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParams p, i64 n_wide) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* base = reinterpret_cast<float*>(smem_raw);
+  int idx;
+  for (;;) {
+    idx = next_item<W>(p.counter, reinterpret_cast<int*>(base));
+    if (idx >= n_wide) break;
+    dsgbsv_system<W>(p, p.order ? p.order[idx] : idx, base);
+    __syncthreads();
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* ws = base + w * p.group_elems;
+  int my = w == 0 ? idx : -1;
+  for (;;) {
+    if (my < 0) {
+      int v = 0;
+      if (lane == 0) v = atomicAdd(p.counter, 1);
+      my = __shfl_sync(0xffffffffu, v, 0);
+    }
+    if (my >= p.count) break;
+    dsgbsv_system<1>(p, p.order ? p.order[my] : my, ws);
+    my = -1;
+  }
+}
+
+// Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window,
+// FP32 solve chunk, FP64 residual scratch; 0 when the refined solve does not support
+// the band (kl + ku above the residual window).
+static i64 mixed_group_elems(i64 kl, i64 ku) {
+  if (kl + ku + 32 > 32 * kResQ) return 0;
+  const i64 f = std::max(std::max(gbtrf_smem_elems<4>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku)),
+                         (i64)(kHdr + 16));
+  return ((f + 3) / 4) * 4;
+}
+
+template <int W>
+static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
+  const i64 we = sc.n_wide > 0 ? mixed_group_elems(sc.wide_kl, sc.wide_ku) : 1;
+  const i64 ne = sc.n_wide < p.count ? mixed_group_elems(sc.narrow_kl, sc.narrow_ku) : 1;
+  if (we == 0 || ne == 0) {
+    set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQ - 32);
+    return BM_ERR_UNSUPPORTED;
+  }
+  p.group_elems = sc.n_wide < p.count ? ne : 0;
+  const i64 bytes = std::max(std::max(we, W * (sc.n_wide < p.count ? ne : 0)), (i64)kHdr) * 4;
+  if (bytes > 227 * 1024) {
+    set_error("%s: the schedule's shared memory (%lld bytes) exceeds the per-CTA limit", name, (long long)bytes);
+    return BM_ERR_UNSUPPORTED;
+  }
+  const void* kfn = (const void*)dsgbsv_batched_kernel<W>;
+  int r = cuda_status(ensure_smem(kfn, (int)bytes), name);
+  if (r) return r;
+  int per_sm = 0;
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsgbsv_batched_kernel<W>, 32 * W, (int)bytes),
+                  name);
+  if (r) return r;
+  per_sm = std::max(per_sm, 1);
+  const i64 need = sc.n_wide + ceil_div(p.count - sc.n_wide, (i64)W);
+  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, std::max<i64>(need, 1));
+  r = cuda_status(cudaMemsetAsync(p.counter, 0, sizeof(int32_t), stream), name);
+  if (r) return r;
+  dsgbsv_batched_kernel<W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(p, sc.n_wide);
+  return launch_status(name);
+}
+
+static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, cudaStream_t stream, const char* name) {
   if (p.count < 0) return -1;
   if (!p.descs && p.count) return -2;
+  if (!sc || sc->n_wide < 0 || sc->n_wide > p.count || (sc->warps != 4 && sc->warps != 8) || sc->wide_kl < 0 ||
+      sc->wide_ku < 0 || sc->narrow_kl < 0 || sc->narrow_ku < 0)
+    return -4;
   if (!p.counter) return -14;
   if (!(p.tol >= 0.0)) return -15;
   if (p.maxit < 0) return -16;
-  if (max_kl < 0) return -17;
-  if (max_ku < 0) return -18;
   if (p.count == 0) return BM_OK;
-  const int kl = (int)max_kl, ku = (int)max_ku;
-  // per-warp shared memory: FP32 factor window / FP32 solve chunk / FP64 residual window
-  const i64 f = std::max(std::max(gbtrf_smem_elems<4>(kl, ku), gbtrs_smem_elems(kl, ku)), (i64)(kHdr + 16));
-  if (kl + ku + 32 > 32 * kResQ) {
-    set_error("%s: kl + ku = %d exceeds the refined solve's limit of %d", name, kl + ku, 32 * kResQ - 32);
-    return BM_ERR_UNSUPPORTED;
-  }
-  const i64 welems = ((f + 3) / 4) * 4;
-  const i64 wbytes = welems * 4;
-  if (wbytes > 227 * 1024) {
-    set_error("%s: widest band of the batch exceeds the per-warp window limit", name);
-    return BM_ERR_UNSUPPORTED;
-  }
-  p.group_elems = welems;
-  const bool cta = (kl + 1) * (kl + ku + 1) >= 512;
-  const int gpc = cta ? 1 : (int)std::max<i64>(1, std::min<i64>(4, (100 * 1024) / wbytes));
-  const int threads = cta ? 128 : 32 * gpc;
-  const int smem = (int)(gpc * wbytes);
-  const void* kfn = cta ? (const void*)dsgbsv_batched_kernel<4> : (const void*)dsgbsv_batched_kernel<1>;
-  int r = cuda_status(ensure_smem(kfn, smem), name);
-  if (r) return r;
-  int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem), name);
-  if (r) return r;
-  per_sm = std::max(per_sm, 1);
-  const i64 grid = std::min<i64>((i64)num_sms() * per_sm, ceil_div(p.count, gpc));
-  r = cuda_status(cudaMemsetAsync(p.counter, 0, sizeof(int32_t), stream), name);
-  if (r) return r;
-  if (cta)
-    dsgbsv_batched_kernel<4><<<(unsigned)grid, threads, smem, stream>>>(p);
-  else
-    dsgbsv_batched_kernel<1><<<(unsigned)grid, threads, smem, stream>>>(p);
-  return launch_status(name);
+  if (sc->warps == 8) return dsgbsv_launch<8>(p, *sc, stream, name);
+  return dsgbsv_launch<4>(p, *sc, stream, name);
 }
 
 }  // namespace bm
@@ -289,5 +319,26 @@ extern "C" int bm_dsgbsv_batched(int64_t count, const bm_gb_desc* descs, const i
   p.maxit = (int)std::min<int64_t>(maxit, 1 << 20);
   p.group_elems = 0;
   if (maxit < 0) return -15;
-  return bm::dsgbsv_batched_impl(p, max_kl, max_ku, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched");
+  if (max_kl < 0) return -17;
+  if (max_ku < 0) return -18;
+  bm_gb_schedule sc;  // every system wide (4 warps) once the widest window holds 512 entries, else narrow
+  sc.n_wide = (max_kl + 1) * (max_kl + max_ku + 1) >= 512 ? count : 0;
+  sc.warps = 4;
+  sc.wide_kl = sc.narrow_kl = max_kl;
+  sc.wide_ku = sc.narrow_ku = max_ku;
+  const int r = bm::dsgbsv_batched_impl(p, &sc, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched");
+  return r == -4 ? -17 : r;
+}
+
+extern "C" int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, const int32_t* order,
+                                       const bm_gb_schedule* sched, const double* AB, const double* B, double* X,
+                                       int64_t* ipiv, int64_t* info, float* AB32, float* R32, int32_t* iters,
+                                       double* berr, int32_t* counter, double tol, int64_t maxit, bm_stream_t stream) {
+  bm::MixedParams p;
+  p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
+  p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
+  p.maxit = (int)std::min<int64_t>(maxit, 1 << 20);
+  p.group_elems = 0;
+  if (maxit < 0) return -16;
+  return bm::dsgbsv_batched_impl(p, sched, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched_sched");
 }

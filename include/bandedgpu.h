@@ -184,6 +184,27 @@ int bm_dgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *orde
 int bm_sgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, float *AB, int64_t *ipiv,
                      float *B, int64_t *info, int32_t *counter, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
 
+/* Launch schedule of a batched solve.  order[0..n_wide) ("wide" systems) are solved
+ * one at a time by a CTA of `warps` (4 or 8) warps; order[n_wide..count) ("narrow")
+ * one per warp, each warp taking the next narrow system as it finishes.  wide_kl/ku
+ * and narrow_kl/ku bound the bandwidths of each part (shared memory is sized from
+ * them).  The host mirror's autotuner (BandedBatch.tune) times candidate schedules
+ * on the batch itself and keeps the fastest. */
+typedef struct {
+  int64_t n_wide;
+  int64_t warps;
+  int64_t wide_kl, wide_ku;
+  int64_t narrow_kl, narrow_ku;
+} bm_gb_schedule;
+
+/* bm_{d,s}gbsv_batched with an explicit schedule (sched: host pointer, read during
+ * the call; order must list the wide systems first).  Graph-capturable like the
+ * single-part entry points. */
+int bm_dgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const bm_gb_schedule *sched,
+                           double *AB, int64_t *ipiv, double *B, int64_t *info, int32_t *counter, bm_stream_t stream);
+int bm_sgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const bm_gb_schedule *sched,
+                           float *AB, int64_t *ipiv, float *B, int64_t *info, int32_t *counter, bm_stream_t stream);
+
 /* Mixed-precision refined batched solve (LAPACK DSGESV's scheme on band storage):
  * each system's FP64 band (AB, gbtrf storage, matrix in rows kl..; read only) is
  * rounded to FP32 into AB32 (same offsets) and factored in FP32 with partial
@@ -201,6 +222,12 @@ int bm_dsgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *ord
                       const double *B, double *X, int64_t *ipiv, int64_t *info, float *AB32, float *R32,
                       int32_t *iters, double *berr, int32_t *counter, double tol, int64_t maxit, int64_t max_kl,
                       int64_t max_ku, bm_stream_t stream);
+
+/* bm_dsgbsv_batched with an explicit schedule (see bm_gb_schedule). */
+int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const bm_gb_schedule *sched,
+                            const double *AB, const double *B, double *X, int64_t *ipiv, int64_t *info, float *AB32,
+                            float *R32, int32_t *iters, double *berr, int32_t *counter, double tol, int64_t maxit,
+                            bm_stream_t stream);
 
 /* Allocation-free variant of bm_dgbsv_batched, for callers that cannot allocate
  * device memory when they solve: code running under CUDA stream capture, real-time

@@ -234,3 +234,87 @@ def test_batched_graph_replay(bm, gpu):
         g.replay()
         torch.cuda.synchronize()
         assert torch.equal(batch.B, ref)
+
+
+def _uneven_batch(bm, gpu, seed, count, n_hi, band_hi, dt=torch.float64):
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(16), np.log(n_hi), count)).astype(np.int64)
+    kl = rng.integers(0, band_hi + 1, count)
+    ku = rng.integers(0, band_hi + 1, count)
+    nrhs = rng.integers(1, 9, count)
+    batch = bm.BandedBatch(n, kl, ku, nrhs, dt, gpu)
+    g = torch.Generator(device=gpu)
+    g.manual_seed(seed)
+    for s in range(count):
+        mb = batch.matrix_band(s)
+        mb.normal_(generator=g)
+        mb[int(ku[s])] += 2.0 * (kl[s] + ku[s]) + 1.0
+        batch.rhs(s).normal_(generator=g)
+    return batch
+
+
+@pytest.mark.parametrize("tdt", [torch.float64, torch.float32])
+def test_batched_schedules_bitexact(bm, gpu, tdt):
+    """Two-part schedules (CTA width 4/8, any narrow/wide split) give the default
+    launch's factors, pivots and solutions bit for bit: the group size only
+    distributes the same operations."""
+    batch = _uneven_batch(bm, gpu, 21, 120, 900, 70, tdt)
+    AB0, B0 = batch.AB.clone(), batch.B.clone()
+    batch.factor_solve()
+    ref = (batch.AB.clone(), batch.ipiv.clone(), batch.B.clone(), batch.info.clone())
+    ran = 0
+    for warps in (4, 8):
+        for cols in (0, 12, 33, 64, 1 << 30):
+            batch.AB.copy_(AB0)
+            batch.B.copy_(B0)
+            batch.set_schedule(warps, cols)
+            try:
+                batch.factor_solve()
+            except bm.BandedGPUError:  # this split's narrow slices do not fit in shared memory
+                continue
+            torch.cuda.synchronize()
+            ran += 1
+            got = (batch.AB, batch.ipiv, batch.B, batch.info)
+            for a, b in zip(got, ref):
+                assert torch.equal(a, b), (warps, cols)
+    assert ran >= 6
+    batch.set_schedule(None)
+
+
+def test_batched_tune_picks_a_schedule_and_keeps_inputs(bm, gpu):
+    """The autotuner times the candidates on the batch, restores its inputs and leaves
+    the fastest schedule set; solving afterwards still gives the default results."""
+    batch = _uneven_batch(bm, gpu, 22, 200, 1200, 48)
+    AB0, B0 = batch.AB.clone(), batch.B.clone()
+    batch.factor_solve()
+    ref = batch.B.clone()
+    batch.AB.copy_(AB0)
+    batch.B.copy_(B0)
+    best = batch.tune("plain")
+    assert torch.equal(batch.AB, AB0) and torch.equal(batch.B, B0)
+    assert best["warps"] in (4, 8) and len(best["candidates"]) >= 6
+    assert best["ms"] == min(c["ms"] for c in best["candidates"])
+    batch.factor_solve()
+    assert torch.equal(batch.B, ref)
+    again = batch.tune("plain")  # cached per batch shape
+    assert again is best or again == best
+
+
+def test_mixed_schedules_identical(bm, gpu):
+    """The refined solve gives identical solutions, iterations and backward errors
+    under every schedule."""
+    batch = _uneven_batch(bm, gpu, 23, 96, 1500, 60)
+    batch.solve_mixed(1e-10, 30)
+    torch.cuda.synchronize()
+    X0, it0, be0 = batch.X.clone(), batch.iters.clone(), batch.berr.clone()
+    for warps in (4, 8):
+        for cols in (0, 24, 1 << 30):
+            batch.set_schedule(warps, cols)
+            try:
+                batch.solve_mixed(1e-10, 30)
+            except bm.BandedGPUError:
+                continue
+            torch.cuda.synchronize()
+            assert torch.equal(batch.X, X0) and torch.equal(batch.iters, it0) and torch.equal(batch.berr, be0), \
+                (warps, cols)
+    assert batch.berr.max().item() <= 1e-10
