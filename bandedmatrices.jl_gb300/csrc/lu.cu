@@ -20,6 +20,14 @@ __global__ void __launch_bounds__(32 * G) gbtrf_one_kernel(i64 m, i64 n, int kl,
 }
 
 template <typename T, int G>
+__global__ void __launch_bounds__(32 * G) gbtrf_blocked_one_kernel(i64 m, i64 n, int kl, int ku, T* ab, i64 ldab,
+                                                                   i64* ipiv, i64* info) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const i64 r = gbtrf_blocked_group<T, G>(m, n, kl, ku, ab, ldab, ipiv, reinterpret_cast<T*>(smem_raw));
+  if (threadIdx.x == 0) *info = r;
+}
+
+template <typename T, int G>
 __global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* ab,
                                                            i64 ldab, const i64* ipiv, T* B, i64 ldb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -94,6 +102,21 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
   if (m == 0 || n == 0) return cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
   if (!ipiv) return -7;
   const i64 bytes = gbtrf_smem_elems<kP>((int)kl, (int)ku) * (i64)sizeof(T);
+  const i64 bbytes = gbtrf_blocked_smem_elems<T>((int)kl, (int)ku) * (i64)sizeof(T);
+  // the one-column step where its window fits (measured faster); panels of kNB
+  // columns where only the panel window fits
+  if (bytes > 227 * 1024 && bbytes <= 227 * 1024) {
+    if (kl + ku + 1 > 128) {
+      int r = cuda_status(ensure_smem((const void*)gbtrf_blocked_one_kernel<T, 8>, (int)bbytes), name);
+      if (r) return r;
+      gbtrf_blocked_one_kernel<T, 8><<<1, 256, (int)bbytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+    } else {
+      int r = cuda_status(ensure_smem((const void*)gbtrf_blocked_one_kernel<T, 4>, (int)bbytes), name);
+      if (r) return r;
+      gbtrf_blocked_one_kernel<T, 4><<<1, 128, (int)bbytes, stream>>>(m, n, (int)kl, (int)ku, ab, ldab, ipiv, info);
+    }
+    return launch_status(name);
+  }
   if (bytes > 227 * 1024) {
     set_error("%s: band (kl=%lld, ku=%lld) exceeds the single-system window limit", name, (long long)kl,
               (long long)ku);
@@ -149,7 +172,7 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
 
 // Shared memory of one group solving systems up to (kl, ku), 16-byte rounded, in T.
 template <typename T>
-static i64 group_elems(i64 kl, i64 ku) {
+static i64 group_elems(i64 kl, i64 ku, bool /*wide*/) {
   const i64 e = std::max(gbtrf_smem_elems<kP>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku));
   return ((e * (i64)sizeof(T) + 15) / 16) * 16 / (i64)sizeof(T);
 }
@@ -158,8 +181,8 @@ template <typename T, int W>
 static int gbsv_batched_launch(i64 count, const bm_gb_desc* descs, const int32_t* order, const bm_gb_schedule& sc,
                                T* AB, i64* ipiv, T* B, i64* info, int32_t* counter, cudaStream_t stream,
                                const char* name) {
-  const i64 we = sc.n_wide > 0 ? group_elems<T>(sc.wide_kl, sc.wide_ku) : 0;
-  const i64 ne = sc.n_wide < count ? group_elems<T>(sc.narrow_kl, sc.narrow_ku) : 0;
+  const i64 we = sc.n_wide > 0 ? group_elems<T>(sc.wide_kl, sc.wide_ku, true) : 0;
+  const i64 ne = sc.n_wide < count ? group_elems<T>(sc.narrow_kl, sc.narrow_ku, false) : 0;
   const i64 elems = std::max(std::max(we, W * ne), (i64)kHdr);
   const i64 bytes = elems * (i64)sizeof(T);
   if (bytes > 227 * 1024) {

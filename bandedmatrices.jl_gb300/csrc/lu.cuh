@@ -359,6 +359,172 @@ __device__ i64 gbtrf_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64
   return info;
 }
 
+// ------------------------------------------------------------ blocked gbtrf
+// The same factorization in panels of NB columns, for one group of G > 1 warps.
+// dgbtf2 gives every element of a column the same sequence per elimination step k:
+// the interchange of rows k and k+jp_k, then (for a nonzero pivot and u_k != 0)
+// a <- fma(l, -u_k, a) on the rows k+1 .. k+km_k.  The blocked order keeps each
+// column's sequence and only regroups columns:
+//   * the panel's NB columns take their steps one by one (the interchange of step c
+//     over columns c..NB-1 of the panel, the scaling of column c, the rank-1 update of
+//     the later panel columns), as dgbtf2 does;
+//   * every trailing column then replays the panel's steps k = 0..NB-1 in order --
+//     interchange, then its update from the stored multipliers of step k -- one thread
+//     per column, all columns at once;
+// so factors and pivots equal dgbtf2's bit for bit while the steps that cannot be
+// parallelised touch only NB columns.  L columns are stored as each step leaves them
+// (dgbtf2's format); U rows when the panel is done.
+//
+// The window holds rows j0 .. j0+R-1, R = kl+NB, and columns j0 .. j0+C-1, C = kl+ku+NB,
+// of the partially factored matrix, as a ring in both dimensions (row r at physical
+// (rb + r) mod R, column c at (cb + c) mod C, column stride RS = R|1).
+constexpr int kNB = 16;
+template <typename T>
+__host__ __device__ inline i64 gbtrf_blocked_smem_elems(int kl, int ku) {
+  const int R = kl + kNB, C = kl + ku + kNB;
+  return kHdr + (i64)(R | 1) * C + 2 * kNB;  // header + window + the panel's pivots and flags
+}
+
+template <typename T, int G>
+__device__ i64 gbtrf_blocked_group(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab,
+                                   i64* __restrict__ ipiv, T* __restrict__ smem) {
+  static_assert(G > 1, "blocked gbtrf runs on a whole CTA");
+  constexpr int NT = Grp<G>::NT, NB = kNB;
+  const int tid = threadIdx.x, lane = tid & 31, wig = tid >> 5;
+  const int kv = kl + ku, R = kl + NB, C = kv + NB, RS = R | 1;
+  int* hdr = reinterpret_cast<int*>(smem);
+  T* W = smem + kHdr;
+  int* JP = reinterpret_cast<int*>(W + (i64)RS * C);  // per panel step: pivot offset,
+  int* NS = JP + kNB;                                  // and whether the pivot is nonzero
+  const i64 mn = min(m, n);
+  i64 info = 0;
+  if (mn <= 0) return 0;
+  int rb = 0, cb = 0;
+  auto prow = [&](int r) { int q = rb + r; return q >= R ? q - R : q; };
+  auto pcol = [&](int c) { int q = cb + c; return q >= C ? q - C : q; };
+  // A(i, c) of the original band (zero outside it); i, c are matrix indices
+  auto orig = [&](i64 i, i64 c) -> T {
+    return (i < m && c < n && i - c <= kl && c - i <= ku) ? ab[(kv + i - c) + c * ldab] : T(0);
+  };
+  // initial window: matrix rows 0..R-1, columns 0..C-1
+  for (int e = tid; e < R * C; e += NT) {
+    const int c = e / R, r = e - c * R;
+    W[r + c * RS] = orig(r, c);
+  }
+  __syncthreads();
+
+  for (i64 j0 = 0; j0 < mn; j0 += NB) {
+    const int jb = (int)min((i64)NB, mn - j0);
+    // ---- panel: steps c = 0..jb-1 on columns [0, jb) (interchanges over all columns)
+    for (int c = 0; c < jb; ++c) {
+      const i64 gj = j0 + c;
+      const int km = (int)min((i64)kl, m - 1 - gj);
+      T* colc = W + pcol(c) * RS;
+      if (wig == 0) {  // idamax over rows c..c+km
+        unsigned long long key = 0ull;
+        int idx = 0x7fffffff;
+        for (int r = lane; r <= km; r += 32) {
+          const unsigned long long k = pivot_key(colc[prow(c + r)], r == 0);
+          if (idx == 0x7fffffff || k > key) {
+            key = k;
+            idx = r;
+          }
+        }
+        const int jp = warp_argmax_first(key, idx);
+        if (lane == 0) {
+          hdr[0] = jp;
+          JP[c] = jp;
+          NS[c] = is_nonzero(colc[prow(c + jp)]) ? 1 : 0;
+          ipiv[gj] = gj + jp + 1;
+        }
+      }
+      __syncthreads();
+      const int jp = hdr[0];
+      const int pr0 = prow(c), prp = prow(c + jp);
+      const T piv = colc[prp];
+      const bool nonsingular = is_nonzero(piv);
+      if (nonsingular && jp != 0)  // interchange rows c and c+jp in panel columns c..jb-1
+        for (int t = c + tid; t < jb; t += NT) {
+          T* col = W + pcol(t) * RS;
+          const T a = col[pr0];
+          col[pr0] = col[prp];
+          col[prp] = a;
+        }
+      __syncthreads();
+      if (nonsingular) {
+        const T rcp = T(1) / piv;
+        for (int r = 1 + tid; r <= km; r += NT) colc[prow(c + r)] = rcp * colc[prow(c + r)];
+      } else if (info == 0) {
+        info = gj + 1;
+      }
+      __syncthreads();
+      for (int r = 1 + tid; r <= km; r += NT) ab[(kv + r) + gj * ldab] = colc[prow(c + r)];  // L(gj+r, gj)
+      // rank-1 update of the panel's later columns: thread per (row, column) pair
+      if (nonsingular) {
+        const int nc = jb - 1 - c;
+        for (int e = tid; e < km * nc; e += NT) {
+          const int cc = c + 1 + e / km, r = c + 1 + e % km;
+          T* col = W + pcol(cc) * RS;
+          const T u = col[pr0];
+          if (is_nonzero(u)) col[prow(r)] = fma(colc[prow(r)], -u, col[prow(r)]);
+        }
+      }
+      __syncthreads();
+    }
+    // ---- trailing columns [jb, C): each replays the panel's steps in order
+    for (int t = jb + tid; t < C; t += NT) {
+      T* col = W + pcol(t) * RS;
+      for (int k = 0; k < jb; ++k) {
+        if (!NS[k]) continue;  // a zero pivot: no interchange, no update
+        const int pk = prow(k);
+        T u = col[pk];
+        if (JP[k] != 0) {
+          const int pp = prow(k + JP[k]);
+          const T v = col[pp];
+          col[pp] = u;
+          u = v;
+          col[pk] = u;
+        }
+        if (!is_nonzero(u)) continue;
+        const T nu = -u;
+        const T* lk = W + pcol(k) * RS;
+        const int len = (int)min((i64)kl, m - 1 - (j0 + k));  // rows k+1 .. k+km_k
+        const int p1 = prow(k + 1 >= R ? k + 1 - R : k + 1);  // physical row of k+1
+        const int s1 = min(len, R - p1);                        // rows before the wrap
+        rank1_run<T>(col + p1, lk + p1, s1, nu);
+        rank1_run<T>(col, lk, len - s1, nu);
+      }
+    }
+    __syncthreads();
+    // ---- U rows j0 .. j0+jb-1 to global; U(gj, gj+c') = window (r, r + c'), c' <= kv
+    for (int e = tid; e < jb * (kv + 1); e += NT) {
+      const int r = e / (kv + 1), d = e - r * (kv + 1);
+      const i64 gi = j0 + r, gc = gi + d;
+      if (gc < n) ab[(kv - d) + gc * ldab] = W[pcol(r + d) * RS + prow(r)];
+    }
+    if (j0 + jb >= mn) break;
+    __syncthreads();
+    // ---- slide by NB: rows j0+R.. and columns j0+C.. enter (original band, zero
+    // elsewhere) into the slots rows/columns 0..NB-1 leave
+    const i64 nj = j0 + NB;
+    for (int e = tid; e < NB * C; e += NT) {  // new rows, every new-frame column
+      const int rr = e / C, c = e - rr * C;   // new-frame row R-NB+rr, column c
+      const int pr = prow(rr), pc = pcol(NB + c >= C ? NB + c - C : NB + c);
+      W[pc * RS + pr] = orig(nj + R - NB + rr, nj + c);
+    }
+    for (int e = tid; e < NB * (R - NB); e += NT) {  // new columns, old rows that stay
+      const int cc = e / (R - NB), r = e - cc * (R - NB);  // new-frame column C-NB+cc, row r
+      const int pc = pcol(cc), pr = prow(NB + r);
+      W[pc * RS + pr] = orig(nj + r, nj + C - NB + cc);
+    }
+    __syncthreads();
+    rb = prow(NB);
+    cb = pcol(NB);
+  }
+  __syncthreads();
+  return info;
+}
+
 // --------------------------------------------------------------------- gbtrs
 // Thread layout for a group of nr <= kMaxRhs right-hand sides: nr is padded to a
 // power of two 1 << lg; thread -> (row offset tid >> lg, column tid & ((1<<lg)-1)),
@@ -367,27 +533,49 @@ __device__ __forceinline__ int rhs_lg(int nr) { return nr <= 1 ? 0 : nr <= 2 ? 1
 
 // Solves op(A) X = B for nr <= kMaxRhs right-hand sides (B: n x nr, leading dim ldb)
 // with the gbtrf factors; trans: false = 'N', true = 'T'.
+//
+// The sweeps run in chunks of kChunk steps.  At a chunk boundary the whole group
+// stages the chunk's L or U columns (LC), its pivots (IP) and the rows of b the chunk
+// needs (window X, row-major over the nr columns); inside a chunk each warp sweeps its
+// own right-hand-side columns (warp w: columns [w*q, (w+1)*q), q = ceil(nr/G)) with
+// only warp-level synchronisation.  Every element receives its updates in dgbtrs /
+// dtbsv order.
 template <typename T, int G>
 __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* __restrict__ ab, i64 ldab,
                             const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem) {
   constexpr int NT = Grp<G>::NT;
   const int tid = Grp<G>::tid(), lane = threadIdx.x & 31, wig = tid >> 5;
   const int kv = kl + ku;
-  const int lg = rhs_lg(nr), cl = tid & ((1 << lg) - 1), rstep = NT >> lg, r0 = tid >> lg;
-  const bool cok = cl < nr;
+  // this warp's columns and its lane layout: lane -> (column cw0 + (lane & (2^lg-1)),
+  // first row lane >> lg), rows advancing by 32 >> lg
+  const int q = (nr + G - 1) / G;
+  const int cw0 = min(nr, wig * q), nw = min(nr, cw0 + q) - cw0;
+  const int lg = rhs_lg(nw), cl = cw0 + (lane & ((1 << lg) - 1)), rstep = 32 >> lg, r0 = lane >> lg;
+  const bool cok = nw > 0 && (lane & ((1 << lg) - 1)) < nw;
+  const bool own = lane < nw;  // lanes that own one whole column (cw0 + lane)
+  const int oc = cw0 + lane;
   i64* IP = reinterpret_cast<i64*>(smem + kHdr);  // kChunk pivots (8-byte aligned)
   T* X = smem + kHdr + 2 * kChunk;                // window: XW rows x nr
   const int XW = kChunk + kv + 1;
   T* LC = X + XW * kMaxRhs;                       // kChunk columns x (kv+1)
-  auto sync = [] { Grp<G>::sync(); };
-  // copy window rows [s0, s1) from/to b rows [g0 + s0, ...), zero outside [0, n)
+  auto gsync = [] { Grp<G>::sync(); };
+  // group-cooperative copies of window rows [s0, s1) from/to b rows g0 + s0 .. (zero
+  // outside [0, n))
   auto load_rows = [&](int s0, int s1, i64 g0) {
-    for (int sr = s0 + r0; sr < s1; sr += rstep)
-      if (cok) X[sr * nr + cl] = (g0 + sr >= 0 && g0 + sr < n) ? b[(g0 + sr) + cl * ldb] : T(0);
+    const int cnt = (s1 - s0) * nr;
+    for (int e = tid; e < cnt; e += NT) {
+      const int sr = s0 + e / nr, c = e - (e / nr) * nr;
+      const i64 g = g0 + sr;
+      X[sr * nr + c] = (g >= 0 && g < n) ? b[g + c * ldb] : T(0);
+    }
   };
   auto store_rows = [&](int s0, int s1, i64 g0) {
-    for (int sr = s0 + r0; sr < s1; sr += rstep)
-      if (cok && g0 + sr >= 0 && g0 + sr < n) b[(g0 + sr) + cl * ldb] = X[sr * nr + cl];
+    const int cnt = (s1 - s0) * nr;
+    for (int e = tid; e < cnt; e += NT) {
+      const int sr = s0 + e / nr, c = e - (e / nr) * nr;
+      const i64 g = g0 + sr;
+      if (g >= 0 && g < n) b[g + c * ldb] = X[sr * nr + c];
+    }
   };
 
   if (!trans) {
@@ -402,33 +590,36 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
           LC[sidx * kl + i] = (j0 + sidx + 1 + i < n) ? ab[(kv + 1 + i) + (j0 + sidx) * ldab] : T(0);
         }
         for (int sidx = tid; sidx < jn; sidx += NT) IP[sidx] = ipiv[j0 + sidx] - 1 - j0;
-        sync();
-        for (int st = 0; st < jn; ++st) {
-          const int lm = (int)min((i64)kl, n - 1 - (j0 + st));
-          const int l = (int)IP[st];
-          if (l != st) {
-            if (tid < nr) {
-              const T t = X[l * nr + tid];
-              X[l * nr + tid] = X[st * nr + tid];
-              X[st * nr + tid] = t;
+        gsync();
+        if (nw > 0) {
+          for (int st = 0; st < jn; ++st) {
+            const int lm = (int)min((i64)kl, n - 1 - (j0 + st));
+            const int l = (int)IP[st];
+            if (l != st) {
+              if (own) {
+                const T t = X[l * nr + oc];
+                X[l * nr + oc] = X[st * nr + oc];
+                X[st * nr + oc] = t;
+              }
+              __syncwarp();
             }
-            sync();
-          }
-          if (cok) {
-            const T bj = X[st * nr + cl];
-            if (bj != T(0)) {
-              const T t = -bj;
-              for (int i = r0; i < lm; i += rstep)
-                X[(st + 1 + i) * nr + cl] = fma(LC[st * kl + i], t, X[(st + 1 + i) * nr + cl]);
+            if (cok) {
+              const T bj = X[st * nr + cl];
+              if (bj != T(0)) {
+                const T t = -bj;
+                for (int i = r0; i < lm; i += rstep)
+                  X[(st + 1 + i) * nr + cl] = fma(LC[st * kl + i], t, X[(st + 1 + i) * nr + cl]);
+              }
             }
+            __syncwarp();
           }
-          sync();
         }
+        gsync();
         store_rows(0, jn, j0);
-        sync();
+        gsync();
         grp_shift_down<T, G>(X, kl * nr, jn * nr);  // carry rows jn .. jn+kl to the front
         if (j0 + jn >= n - 1) store_rows(0, kl, j0 + jn);
-        sync();
+        gsync();
       }
     }
     // ---- backward: U x = y (dtbsv 'U','N','N', bandwidth kv), columns n-1 .. 0;
@@ -436,7 +627,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     i64 j1 = n - 1;
     i64 base = j1 - (XW - 1);
     load_rows(0, XW, base);
-    sync();
+    gsync();
     while (true) {
       const int jn = (int)min((i64)kChunk, j1 + 1);
       // U(j-i, j) = ab[(kv-i) + j*ldab], i = 0..kv, for j = j1, j1-1, ...
@@ -445,39 +636,42 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
         const i64 j = j1 - t;
         LC[e] = (j - i >= 0) ? ab[(kv - i) + j * ldab] : T(0);
       }
-      sync();
-      for (int t = 0; t < jn; ++t) {
-        const i64 j = j1 - t;
-        const int xs = (int)(j - base);
-        if (tid < nr) {
-          const T xv = X[xs * nr + tid];
-          if (xv != T(0)) X[xs * nr + tid] = xv / LC[t * (kv + 1)];
-        }
-        sync();
-        if (cok) {
-          const T xj = X[xs * nr + cl];
-          if (xj != T(0)) {
-            const T tt = -xj;
-            const int lim = (int)min((i64)kv, j);
-            for (int i = 1 + r0; i <= lim; i += rstep)
-              X[(xs - i) * nr + cl] = fma(tt, LC[t * (kv + 1) + i], X[(xs - i) * nr + cl]);
+      gsync();
+      if (nw > 0) {
+        for (int t = 0; t < jn; ++t) {
+          const i64 j = j1 - t;
+          const int xs = (int)(j - base);
+          if (own) {
+            const T xv = X[xs * nr + oc];
+            if (xv != T(0)) X[xs * nr + oc] = xv / LC[t * (kv + 1)];
           }
+          __syncwarp();
+          if (cok) {
+            const T xj = X[xs * nr + cl];
+            if (xj != T(0)) {
+              const T tt = -xj;
+              const int lim = (int)min((i64)kv, j);
+              for (int i = 1 + r0; i <= lim; i += rstep)
+                X[(xs - i) * nr + cl] = fma(tt, LC[t * (kv + 1) + i], X[(xs - i) * nr + cl]);
+            }
+          }
+          __syncwarp();
         }
-        sync();
       }
+      gsync();
       store_rows((int)(j1 - jn + 1 - base), (int)(j1 + 1 - base), base);
-      sync();
+      gsync();
       j1 -= jn;
       if (j1 < 0) break;
       grp_shift_up<T, G>(X, (XW - jn) * nr, jn * nr);
       base -= jn;
       load_rows(0, jn, base);
-      sync();
+      gsync();
     }
   } else {
     // ---- U^T y = b (dtbsv 'U','T','N') in axpy form: once x_i is final, x_c -= U(i,c) x_i
     load_rows(0, XW, 0);
-    sync();
+    gsync();
     for (i64 j0 = 0; j0 < n; j0 += kChunk) {
       const int jn = (int)min((i64)kChunk, n - j0);
       // row i of U: U(i, i+c) = ab[(kv-c) + (i+c)*ldab], c = 0..kv
@@ -486,55 +680,97 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
         const i64 i = j0 + t;
         LC[e] = (i + c < n) ? ab[(kv - c) + (i + c) * ldab] : T(0);
       }
-      sync();
-      for (int t = 0; t < jn; ++t) {
-        const i64 i = j0 + t;
-        if (tid < nr) X[t * nr + tid] = X[t * nr + tid] / LC[t * (kv + 1)];
-        sync();
-        if (cok) {
-          const T xi = X[t * nr + cl];
-          const int lim = (int)min((i64)kv, n - 1 - i);
-          for (int c = 1 + r0; c <= lim; c += rstep)
-            X[(t + c) * nr + cl] = fma(-LC[t * (kv + 1) + c], xi, X[(t + c) * nr + cl]);
+      gsync();
+      if (nw > 0) {
+        for (int t = 0; t < jn; ++t) {
+          const i64 i = j0 + t;
+          if (own) X[t * nr + oc] = X[t * nr + oc] / LC[t * (kv + 1)];
+          __syncwarp();
+          if (cok) {
+            const T xi = X[t * nr + cl];
+            const int lim = (int)min((i64)kv, n - 1 - i);
+            for (int c = 1 + r0; c <= lim; c += rstep)
+              X[(t + c) * nr + cl] = fma(-LC[t * (kv + 1) + c], xi, X[(t + c) * nr + cl]);
+          }
+          __syncwarp();
         }
-        sync();
       }
+      gsync();
       store_rows(0, jn, j0);
-      sync();
+      gsync();
       grp_shift_down<T, G>(X, (XW - jn) * nr, jn * nr);
       load_rows(XW - jn, XW, j0 + jn);
-      sync();
+      gsync();
     }
-    // ---- L^T with interchanges, j = n-2 .. 0 (dgbtrs 'T': dgemv then dswap)
-    if (kl > 0) {
-      for (i64 j = n - 2; j >= 0; --j) {
-        const int lm = (int)min((i64)kl, n - 1 - j);
-        const T* lc = ab + (kv + 1) + j * ldab;
-        if (kl <= 16) {
-          if (tid < nr) {
-            T temp = T(0);
-            for (int i = 0; i < lm; ++i) temp = fma(b[(j + 1 + i) + tid * ldb], lc[i], temp);
-            b[j + tid * ldb] = fma(T(-1), temp, b[j + tid * ldb]);
-          }
-        } else if (wig == 0) {
-          for (int c = 0; c < nr; ++c) {
-            T temp = T(0);
-            for (int i = lane; i < lm; i += 32) temp = fma(b[(j + 1 + i) + c * ldb], lc[i], temp);
+    // ---- L^T with interchanges, j = n-2 .. 0 (dgbtrs 'T': dgemv then dswap).  Chunk of
+    // steps j = j1 .. j1-jn+1; window rows s <-> b rows base + s, base = j1-jn+1,
+    // holding rows base .. j1+kl; after the chunk, rows above j1-jn+1+kl are final.
+    if (kl > 0 && n > 1) {
+      i64 j1 = n - 2;
+      int jn = (int)min((i64)kChunk, j1 + 1);
+      i64 base = j1 - jn + 1;
+      load_rows(0, jn + kl, base);
+      while (true) {
+        // LC[t][i] = L(j+1+i, j), j = j1 - t; IP[t] = pivot row of j, in the window
+        for (int e = tid; e < jn * kl; e += NT) {
+          const int t = e / kl, i = e - t * kl;
+          const i64 j = j1 - t;
+          LC[e] = (j + 1 + i < n) ? ab[(kv + 1 + i) + j * ldab] : T(0);
+        }
+        for (int t = tid; t < jn; t += NT) IP[t] = ipiv[j1 - t] - 1 - base;
+        gsync();
+        if (nw > 0) {
+          for (int t = 0; t < jn; ++t) {
+            const i64 j = j1 - t;
+            const int s0 = (int)(j - base);
+            const int lm = (int)min((i64)kl, n - 1 - j);
+            const T* lc = LC + t * kl;
+            if (kl <= 16) {  // sequential fma dot product, as reference dgemv 'T'
+              if (own) {
+                T temp = T(0);
+                for (int i = 0; i < lm; ++i) temp = fma(X[(s0 + 1 + i) * nr + oc], lc[i], temp);
+                X[s0 * nr + oc] = fma(T(-1), temp, X[s0 * nr + oc]);
+              }
+            } else {  // warp tree reduction per column
+              for (int c = cw0; c < cw0 + nw; ++c) {
+                T temp = T(0);
+                for (int i = lane; i < lm; i += 32) temp = fma(X[(s0 + 1 + i) * nr + c], lc[i], temp);
 #pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
-            if (lane == 0) b[j + c * ldb] = fma(T(-1), temp, b[j + c * ldb]);
+                for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
+                if (lane == 0) X[s0 * nr + c] = fma(T(-1), temp, X[s0 * nr + c]);
+              }
+            }
+            __syncwarp();
+            const int l = (int)IP[t];
+            if (l != s0 && own) {
+              const T tv = X[l * nr + oc];
+              X[l * nr + oc] = X[s0 * nr + oc];
+              X[s0 * nr + oc] = tv;
+            }
+            __syncwarp();
           }
         }
-        __threadfence_block();
-        sync();
-        const i64 l = ipiv[j] - 1;
-        if (l != j && tid < nr) {
-          const T t = b[l + tid * ldb];
-          b[l + tid * ldb] = b[j + tid * ldb];
-          b[j + tid * ldb] = t;
+        gsync();
+        // rows base + jn - 1 + kl + 1 .. are final: window rows jn + kl - ... ; store the
+        // window's top jn rows that are now final (s >= kl ... window end) and slide down
+        const i64 nb = j1 - jn;  // next chunk's top step
+        if (nb < 0) {
+          store_rows(0, jn + kl, base);
+          gsync();
+          break;
         }
-        __threadfence_block();
-        sync();
+        const int jn2 = (int)min((i64)kChunk, nb + 1);
+        // final rows: b rows > base + kl - 1 + ... = rows base + kl .. base + jn + kl - 1
+        // become final only after the steps they can still be swapped with; steps of the
+        // next chunk touch rows <= nb + kl = base - 1 + kl, so rows base + kl .. are final
+        store_rows(kl, jn + kl, base);
+        gsync();
+        grp_shift_up<T, G>(X, kl * nr, jn2 * nr);  // rows 0..kl-1 move to jn2..jn2+kl-1
+        base = nb - jn2 + 1;
+        j1 = nb;
+        jn = jn2;
+        load_rows(0, jn, base);
+        gsync();
       }
     }
   }

@@ -256,17 +256,18 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
 // Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window,
 // FP32 solve chunk, FP64 residual scratch; 0 when the refined solve does not support
 // the band (kl + ku above the residual window).
-static i64 mixed_group_elems(i64 kl, i64 ku) {
+static i64 mixed_group_elems(i64 kl, i64 ku, bool wide) {
   if (kl + ku + 32 > 32 * kResQ) return 0;
-  const i64 f = std::max(std::max(gbtrf_smem_elems<4>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku)),
-                         (i64)(kHdr + 16));
+  (void)wide;
+  const i64 fac = gbtrf_smem_elems<4>((int)kl, (int)ku);
+  const i64 f = std::max(std::max(fac, gbtrs_smem_elems((int)kl, (int)ku)), (i64)(kHdr + 16));
   return ((f + 3) / 4) * 4;
 }
 
 template <int W>
 static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
-  const i64 we = sc.n_wide > 0 ? mixed_group_elems(sc.wide_kl, sc.wide_ku) : 1;
-  const i64 ne = sc.n_wide < p.count ? mixed_group_elems(sc.narrow_kl, sc.narrow_ku) : 1;
+  const i64 we = sc.n_wide > 0 ? mixed_group_elems(sc.wide_kl, sc.wide_ku, true) : 1;
+  const i64 ne = sc.n_wide < p.count ? mixed_group_elems(sc.narrow_kl, sc.narrow_ku, false) : 1;
   if (we == 0 || ne == 0) {
     set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQ - 32);
     return BM_ERR_UNSUPPORTED;

@@ -318,3 +318,25 @@ def test_mixed_schedules_identical(bm, gpu):
             assert torch.equal(batch.X, X0) and torch.equal(batch.iters, it0) and torch.equal(batch.berr, be0), \
                 (warps, cols)
     assert batch.berr.max().item() <= 1e-10
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("m,n,l,u,zero_cols", [(300, 300, 20, 20, (37, 38)), (260, 200, 25, 9, (16,)),
+                                               (200, 260, 9, 25, (31, 100)), (500, 500, 40, 70, ()),
+                                               (97, 97, 70, 3, (5, 50)), (129, 129, 18, 30, ())])
+def test_cta_lu_panels_singular_and_rectangular(bm, gpu, orc, dt, m, n, l, u, zero_cols):
+    """Bands wide enough for the CTA (panel) factorization: rectangular shapes, zero
+    columns (exact zero pivots inside a panel) -- factors, pivots and info equal
+    dgbtf2's bit for bit."""
+    rng = np.random.default_rng(m + 3 * n + l)
+    data = rng.standard_normal((l + u + 1, n)).astype(dt)
+    for c in zero_cols:
+        data[:, c] = 0.0
+    A = dev_band(bm, data, m, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(m, n, l, u, orc.lu_storage(data, n, l, u))
+    assert F.info == info
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+    got = F.factors.data.cpu().numpy()
+    mask = orc.band_to_dense(np.ones_like(LU), m, l, l + u) != 0
+    assert np.array_equal(orc.band_to_dense(got, m, l, l + u)[mask], orc.band_to_dense(LU, m, l, l + u)[mask])
