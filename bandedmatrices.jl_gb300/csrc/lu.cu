@@ -29,12 +29,222 @@ __global__ void __launch_bounds__(32 * G) gbtrf_blocked_one_kernel(i64 m, i64 n,
 
 template <typename T, int G>
 __global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* ab,
-                                                           i64 ldab, const i64* ipiv, T* B, i64 ldb) {
+                                                           i64 ldab, const i64* ipiv, T* B, i64 ldb, int ch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // block r sweeps right-hand sides [r*kMaxRhs, (r+1)*kMaxRhs)
   for (i64 r = blockIdx.x; r * kMaxRhs < nrhs; r += gridDim.x)
     gbtrs_all<T, G>(trans, n, kl, ku, min((i64)kMaxRhs, nrhs - r * kMaxRhs), ab, ldab, ipiv, B + r * kMaxRhs * ldb,
-                    ldb, reinterpret_cast<T*>(smem_raw));
+                    ldb, reinterpret_cast<T*>(smem_raw), ch);
+}
+
+// ------------------------------------------------------------------ wide bands
+// Bands whose one-column window does not fit one CTA's shared memory (e.g. kl = ku =
+// 512 in Float64): the factorization runs panel by panel over the gbtrf storage in
+// global memory, as two launches per panel of kNB columns.
+//   * gbtrf_panel_kernel (one CTA): loads the panel -- rows j0 .. j0+kl+kNB-1 of its
+//     kNB columns -- into shared memory, takes dgbtf2's steps on it (pivot search,
+//     interchange within the panel's columns from the step's own column on, scaling,
+//     rank-1 update of the panel's later columns), stores it back (L in dgbtf2's
+//     format) with the pivots;
+//   * gbtrf_replay_kernel (one warp per column): every column the panel's steps can
+//     reach (up to kl+ku to its right) replays the steps in order -- interchange, then
+//     the update from the stored multipliers -- on its rows j0 .. j0+kl+kNB-1, kept in
+//     the warp's shared memory; the multipliers are staged once per CTA, and a step's
+//     interchange and zero-pivot flag come from ipiv and the stored U(j,j).
+// Each element therefore receives dgbtf2's sequence of operations: factors and pivots
+// equal the unblocked result bit for bit.
+constexpr int kWideWarps = 8;
+
+// the top kl rows of gbtrf storage (fill-in) start at zero, as dgbtrf sets them
+template <typename T>
+__global__ void zero_fill_kernel(i64 n, int kl, T* ab, i64 ldab) {
+  const i64 total = n * (i64)kl;
+  for (i64 e = (i64)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+    const i64 c = e / kl;
+    ab[(e - c * kl) + c * ldab] = T(0);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab, i64 ldab,
+                                                          i64* ipiv, i64* info) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NT = 256, NB = kNB;
+  const int tid = threadIdx.x, lane = tid & 31, wig = tid >> 5;
+  const int kv = kl + ku, R = kl + NB, RS = R | 1;
+  const i64 mn = min(m, n);
+  const int jb = (int)min((i64)NB, mn - j0);
+  T* P = reinterpret_cast<T*>(smem_raw);  // panel: column c (0..jb-1) x row r (matrix row j0 + r)
+  int* hdr = reinterpret_cast<int*>(P + (i64)RS * NB);
+  // entry (row j0+r, column j0+c) of the storage when it lies in it
+  auto sidx = [&](int r, int c) -> i64 {
+    const i64 i = j0 + r, col = j0 + c;
+    const i64 d = i - col;
+    return (i < m && d >= -kv && d <= kl) ? (kv + d) + col * ldab : (i64)-1;
+  };
+  for (int e = tid; e < R * jb; e += NT) {
+    const int c = e / R, r = e - c * R;
+    const i64 g = sidx(r, c);
+    P[c * RS + r] = g >= 0 ? ab[g] : T(0);
+  }
+  __syncthreads();
+  i64 inf = *info;
+  for (int c = 0; c < jb; ++c) {
+    const i64 gj = j0 + c;
+    const int km = (int)min((i64)kl, m - 1 - gj);
+    T* colc = P + c * RS;
+    if (wig == 0) {
+      unsigned long long key = 0ull;
+      int idx = 0x7fffffff;
+      for (int r = lane; r <= km; r += 32) {
+        const unsigned long long k = pivot_key(colc[c + r], r == 0);
+        if (idx == 0x7fffffff || k > key) {
+          key = k;
+          idx = r;
+        }
+      }
+      const int jp = warp_argmax_first(key, idx);
+      if (lane == 0) {
+        hdr[0] = jp;
+        ipiv[gj] = gj + jp + 1;
+      }
+    }
+    __syncthreads();
+    const int jp = hdr[0];
+    const T piv = colc[c + jp];
+    const bool nonsingular = is_nonzero(piv);
+    if (nonsingular && jp != 0)
+      for (int t = c + tid; t < jb; t += NT) {
+        T* col = P + t * RS;
+        const T a = col[c];
+        col[c] = col[c + jp];
+        col[c + jp] = a;
+      }
+    __syncthreads();
+    if (nonsingular) {
+      const T rcp = T(1) / piv;
+      for (int r = 1 + tid; r <= km; r += NT) colc[c + r] = rcp * colc[c + r];
+    } else if (inf == 0) {
+      inf = gj + 1;
+    }
+    __syncthreads();
+    if (nonsingular) {
+      const int nc = jb - 1 - c;
+      for (int e = tid; e < km * nc; e += NT) {
+        const int cc = c + 1 + e / km, r = c + 1 + e % km;
+        T* col = P + cc * RS;
+        const T u = col[c];
+        if (is_nonzero(u)) col[r] = fma(colc[r], -u, col[r]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < R * jb; e += NT) {
+    const int c = e / R, r = e - c * R;
+    const i64 g = sidx(r, c);
+    if (g >= 0) ab[g] = P[c * RS + r];
+  }
+  if (tid == 0) *info = inf;
+}
+
+// One warp per column t = first + warp index: rows j0 .. j0+R-1 of the column replay
+// the panel's steps.  smem: the panel's multipliers (R x jb, staged per CTA) and one
+// R-row column buffer per warp.
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) gbtrf_replay_kernel(i64 m, i64 n, int kl, int ku, i64 j0,
+                                                                       i64 first, i64 last, T* ab, i64 ldab,
+                                                                       const i64* ipiv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NB = kNB;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int kv = kl + ku, R = kl + NB, RS = R | 1;
+  const i64 mn = min(m, n);
+  const int jb = (int)min((i64)NB, mn - j0);
+  T* L = reinterpret_cast<T*>(smem_raw);  // column k of the panel: L[k*RS + r], rows j0 + r
+  T* colbuf = L + (i64)RS * NB + (i64)w * RS;
+  __shared__ int st[kNB];
+  for (int e = threadIdx.x; e < R * jb; e += blockDim.x) {
+    const int k = e / R, r = e - k * R;
+    const i64 i = j0 + r, col = j0 + k, d = i - col;
+    L[k * RS + r] = (i < m && d >= -kv && d <= kl) ? ab[(kv + d) + col * ldab] : T(0);
+  }
+  if (threadIdx.x < jb) {  // -1: zero pivot (no interchange, no update)
+    const i64 gj = j0 + threadIdx.x;
+    st[threadIdx.x] = is_nonzero(ab[kv + gj * ldab]) ? (int)(ipiv[gj] - 1 - gj) : -1;
+  }
+  __syncthreads();
+  for (i64 t = first + (i64)blockIdx.x * kWideWarps + w; t < last; t += (i64)gridDim.x * kWideWarps) {
+    // the column's rows j0 .. j0+R-1 (zero outside the storage)
+    for (int r = lane; r < R; r += 32) {
+      const i64 i = j0 + r, d = i - t;
+      colbuf[r] = (i < m && d >= -kv && d <= kl) ? ab[(kv + d) + t * ldab] : T(0);
+    }
+    __syncwarp();
+    for (int k = 0; k < jb; ++k) {
+      const int jp = st[k];
+      if (jp < 0) continue;  // zero pivot: no interchange, no update
+      T u = colbuf[k];
+      if (jp != 0) {
+        const T v = colbuf[k + jp];
+        __syncwarp();
+        if (lane == 0) {
+          colbuf[k + jp] = u;
+          colbuf[k] = v;
+        }
+        u = v;
+      }
+      __syncwarp();
+      if (is_nonzero(u)) {
+        const int km = (int)min((i64)kl, m - 1 - (j0 + k));
+        const T nu = -u;
+        const T* lk = L + k * RS;
+        for (int r = k + 1 + lane; r <= k + km; r += 32) colbuf[r] = fma(lk[r], nu, colbuf[r]);
+      }
+      __syncwarp();
+    }
+    for (int r = lane; r < R; r += 32) {
+      const i64 i = j0 + r, d = i - t;
+      if (i < m && d >= -kv && d <= kl) ab[(kv + d) + t * ldab] = colbuf[r];
+    }
+    __syncwarp();
+  }
+}
+
+template <typename T>
+static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
+                           const char* name) {
+  const int R = (int)kl + kNB, RS = R | 1;
+  const i64 pbytes = ((i64)RS * kNB + 16) * (i64)sizeof(T);
+  const i64 rbytes = ((i64)RS * kNB + (i64)RS * kWideWarps) * (i64)sizeof(T);
+  if (pbytes > 227 * 1024 || rbytes > 227 * 1024) {
+    set_error("%s: band (kl=%lld) exceeds the panel limit", name, (long long)kl);
+    return BM_ERR_UNSUPPORTED;
+  }
+  int r = cuda_status(ensure_smem((const void*)gbtrf_panel_kernel<T>, (int)pbytes), name);
+  if (r) return r;
+  r = cuda_status(ensure_smem((const void*)gbtrf_replay_kernel<T>, (int)rbytes), name);
+  if (r) return r;
+  r = cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
+  if (r) return r;
+  if (kl > 0) {
+    const i64 blocks = std::min<i64>(ceil_div(n * kl, 256), (i64)num_sms() * 16);
+    zero_fill_kernel<T><<<(unsigned)blocks, 256, 0, stream>>>(n, (int)kl, ab, ldab);
+    if ((r = launch_status(name))) return r;
+  }
+  const i64 mn = std::min(m, n);
+  for (i64 j0 = 0; j0 < mn; j0 += kNB) {
+    const i64 jb = std::min<i64>(kNB, mn - j0);
+    gbtrf_panel_kernel<T><<<1, 256, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+    if ((r = launch_status(name))) return r;
+    const i64 first = j0 + jb, last = std::min(n, j0 + jb + kl + ku);
+    if (last > first) {
+      const i64 blocks = std::min<i64>(ceil_div(last - first, kWideWarps), (i64)num_sms() * 2);
+      gbtrf_replay_kernel<T><<<(unsigned)blocks, 32 * kWideWarps, (int)rbytes, stream>>>(
+          m, n, (int)kl, (int)ku, j0, first, last, ab, ldab, ipiv);
+      if ((r = launch_status(name))) return r;
+    }
+  }
+  return BM_OK;
 }
 
 // Factor + solve of one system of a batch by a group of G warps.
@@ -117,11 +327,7 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
     }
     return launch_status(name);
   }
-  if (bytes > 227 * 1024) {
-    set_error("%s: band (kl=%lld, ku=%lld) exceeds the single-system window limit", name, (long long)kl,
-              (long long)ku);
-    return BM_ERR_UNSUPPORTED;
-  }
+  if (bytes > 227 * 1024) return gbtrf_wide_impl<T>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
   if (use_cta_group(kl, ku) && kl + ku + 1 > 128) {  // one thread per window column
     int r = cuda_status(ensure_smem((const void*)gbtrf_one_kernel<T, 8>, (int)bytes), name);
     if (r) return r;
@@ -150,22 +356,28 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
   if (ldab < 2 * kl + ku + 1) return -7;
   if (ldb < std::max<i64>(1, n)) return -10;
   if (n == 0 || nrhs == 0) return BM_OK;
-  const i64 bytes = gbtrs_smem_elems((int)kl, (int)ku) * (i64)sizeof(T);
-  if (bytes > 227 * 1024) {
+  const int ch = gbtrs_chunk_for<T>((int)kl, (int)ku, 227 * 1024);
+  if (ch == 0) {
     set_error("%s: band too wide for the staged solve", name);
     return BM_ERR_UNSUPPORTED;
   }
+  const i64 bytes = gbtrs_smem_elems((int)kl, (int)ku, ch) * (i64)sizeof(T);
   const i64 grid = std::min<i64>(ceil_div(nrhs, kMaxRhs), 65535);
-  if ((kl + ku + 1) * std::min<i64>(nrhs, kMaxRhs) >= 256) {
+  if (kl + ku >= 192) {  // wide: the CTA's 8 warps share the rows of few right-hand sides
+    int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T, 8>, (int)bytes), name);
+    if (r) return r;
+    gbtrs_one_kernel<T, 8><<<(unsigned)grid, 256, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab,
+                                                                         ipiv, B, ldb, ch);
+  } else if ((kl + ku + 1) * std::min<i64>(nrhs, kMaxRhs) >= 256) {
     int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T, 4>, (int)bytes), name);
     if (r) return r;
     gbtrs_one_kernel<T, 4><<<(unsigned)grid, 128, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab,
-                                                                         ipiv, B, ldb);
+                                                                         ipiv, B, ldb, ch);
   } else {
     int r = cuda_status(ensure_smem((const void*)gbtrs_one_kernel<T, 1>, (int)bytes), name);
     if (r) return r;
     gbtrs_one_kernel<T, 1><<<(unsigned)grid, 32, (int)bytes, stream>>>(!notr, n, (int)kl, (int)ku, nrhs, ab, ldab,
-                                                                        ipiv, B, ldb);
+                                                                        ipiv, B, ldb, ch);
   }
   return launch_status(name);
 }

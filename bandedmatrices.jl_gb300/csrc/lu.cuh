@@ -113,13 +113,20 @@ __host__ __device__ inline i64 gbtrf_smem_elems(int kl, int ku) {
   return kHdr + (i64)lu_rs(kl) * K + (i64)P * K + (kl + 1);
 }
 
-constexpr int kChunk = 32;  // solve steps staged per chunk
+constexpr int kChunk = 32;  // solve steps staged per chunk (at most)
 constexpr int kMaxRhs = 8;  // right-hand sides swept together
-__host__ __device__ inline i64 gbtrs_smem_elems(int kl, int ku) {
+__host__ __device__ inline i64 gbtrs_smem_elems(int kl, int ku, int ch = kChunk) {
   const int kv = kl + ku;
   // header + ipiv chunk (kChunk int64, as 2*kChunk T slots) + window of b
-  // ((kChunk+kv+1) rows x kMaxRhs) + chunk of L or U columns (kChunk x (kv+1))
-  return kHdr + 2 * kChunk + (i64)(kChunk + kv + 1) * kMaxRhs + (i64)kChunk * (kv + 1);
+  // ((ch+kv+1) rows x kMaxRhs) + chunk of L or U columns (ch x (kv+1))
+  return kHdr + 2 * kChunk + (i64)(ch + kv + 1) * kMaxRhs + (i64)ch * (kv + 1);
+}
+// the largest chunk (<= kChunk) whose solve window fits `bytes` of shared memory, 0 if none
+template <typename T>
+inline int gbtrs_chunk_for(int kl, int ku, i64 bytes) {
+  for (int ch = kChunk; ch >= 1; ch >>= 1)
+    if (gbtrs_smem_elems(kl, ku, ch) * (i64)sizeof(T) <= bytes) return ch;
+  return 0;
 }
 
 // X[s] <- X[s + d] for s in [0, count), d >= 0 (group-cooperative, overlap-safe)
@@ -542,22 +549,34 @@ __device__ __forceinline__ int rhs_lg(int nr) { return nr <= 1 ? 0 : nr <= 2 ? 1
 // dtbsv order.
 template <typename T, int G>
 __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* __restrict__ ab, i64 ldab,
-                            const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem) {
+                            const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem,
+                            int ch = kChunk) {
   constexpr int NT = Grp<G>::NT;
   const int tid = Grp<G>::tid(), lane = threadIdx.x & 31, wig = tid >> 5;
   const int kv = kl + ku;
-  // this warp's columns and its lane layout: lane -> (column cw0 + (lane & (2^lg-1)),
-  // first row lane >> lg), rows advancing by 32 >> lg
-  const int q = (nr + G - 1) / G;
-  const int cw0 = min(nr, wig * q), nw = min(nr, cw0 + q) - cw0;
-  const int lg = rhs_lg(nw), cl = cw0 + (lane & ((1 << lg) - 1)), rstep = 32 >> lg, r0 = lane >> lg;
-  const bool cok = nw > 0 && (lane & ((1 << lg) - 1)) < nw;
-  const bool own = lane < nw;  // lanes that own one whole column (cw0 + lane)
-  const int oc = cw0 + lane;
-  i64* IP = reinterpret_cast<i64*>(smem + kHdr);  // kChunk pivots (8-byte aligned)
+  // Column sets: each warp sweeps its own right-hand sides (warp w: columns
+  // [w*q, (w+1)*q)) with warp-level synchronisation -- or, when there are far fewer
+  // right-hand sides than warps and the band is wide, the whole group shares every
+  // column's rows and synchronises as a group ("row split").
+  const bool split = G > 1 && nr * 4 <= G && kv >= 192;
+  const int SW = split ? NT : 32;           // threads sharing a column set
+  const int sl = split ? tid : lane;        // this thread's index in its set
+  const int q = split ? nr : (nr + G - 1) / G;
+  const int cw0 = split ? 0 : min(nr, wig * q), nw = min(nr, cw0 + q) - cw0;
+  // thread -> (column cw0 + (sl & (2^lg-1)), first row sl >> lg), rows advancing by SW >> lg
+  const int lg = rhs_lg(nw), cl = cw0 + (sl & ((1 << lg) - 1)), rstep = SW >> lg, r0 = sl >> lg;
+  const bool cok = nw > 0 && (sl & ((1 << lg) - 1)) < nw;
+  const bool own = sl < nw;  // threads that own one whole column (cw0 + sl)
+  const int oc = cw0 + sl;
+  auto wsync = [split] {
+    if (split) Grp<G>::sync();
+    else __syncwarp();
+  };
+  const int kCh = ch;                             // this call's chunk
+  i64* IP = reinterpret_cast<i64*>(smem + kHdr);  // chunk pivots (8-byte aligned)
   T* X = smem + kHdr + 2 * kChunk;                // window: XW rows x nr
-  const int XW = kChunk + kv + 1;
-  T* LC = X + XW * kMaxRhs;                       // kChunk columns x (kv+1)
+  const int XW = kCh + kv + 1;
+  T* LC = X + XW * kMaxRhs;                       // chunk columns x (kv+1)
   auto gsync = [] { Grp<G>::sync(); };
   // group-cooperative copies of window rows [s0, s1) from/to b rows g0 + s0 .. (zero
   // outside [0, n))
@@ -582,8 +601,8 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     // ---- forward: L with row interchanges (dgbtrs 'N': dswap + dger per column)
     if (kl > 0 && n > 1) {
       load_rows(0, kl, 0);
-      for (i64 j0 = 0; j0 < n - 1; j0 += kChunk) {
-        const int jn = (int)min((i64)kChunk, n - 1 - j0);
+      for (i64 j0 = 0; j0 < n - 1; j0 += kCh) {
+        const int jn = (int)min((i64)kCh, n - 1 - j0);
         load_rows(kl, jn + kl, j0);
         for (int e = tid; e < jn * kl; e += NT) {
           const int sidx = e / kl, i = e - sidx * kl;
@@ -601,7 +620,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
                 X[l * nr + oc] = X[st * nr + oc];
                 X[st * nr + oc] = t;
               }
-              __syncwarp();
+              wsync();
             }
             if (cok) {
               const T bj = X[st * nr + cl];
@@ -611,7 +630,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
                   X[(st + 1 + i) * nr + cl] = fma(LC[st * kl + i], t, X[(st + 1 + i) * nr + cl]);
               }
             }
-            __syncwarp();
+            wsync();
           }
         }
         gsync();
@@ -629,7 +648,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     load_rows(0, XW, base);
     gsync();
     while (true) {
-      const int jn = (int)min((i64)kChunk, j1 + 1);
+      const int jn = (int)min((i64)kCh, j1 + 1);
       // U(j-i, j) = ab[(kv-i) + j*ldab], i = 0..kv, for j = j1, j1-1, ...
       for (int e = tid; e < jn * (kv + 1); e += NT) {
         const int t = e / (kv + 1), i = e - t * (kv + 1);
@@ -645,7 +664,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
             const T xv = X[xs * nr + oc];
             if (xv != T(0)) X[xs * nr + oc] = xv / LC[t * (kv + 1)];
           }
-          __syncwarp();
+          wsync();
           if (cok) {
             const T xj = X[xs * nr + cl];
             if (xj != T(0)) {
@@ -655,7 +674,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
                 X[(xs - i) * nr + cl] = fma(tt, LC[t * (kv + 1) + i], X[(xs - i) * nr + cl]);
             }
           }
-          __syncwarp();
+          wsync();
         }
       }
       gsync();
@@ -672,8 +691,8 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     // ---- U^T y = b (dtbsv 'U','T','N') in axpy form: once x_i is final, x_c -= U(i,c) x_i
     load_rows(0, XW, 0);
     gsync();
-    for (i64 j0 = 0; j0 < n; j0 += kChunk) {
-      const int jn = (int)min((i64)kChunk, n - j0);
+    for (i64 j0 = 0; j0 < n; j0 += kCh) {
+      const int jn = (int)min((i64)kCh, n - j0);
       // row i of U: U(i, i+c) = ab[(kv-c) + (i+c)*ldab], c = 0..kv
       for (int e = tid; e < jn * (kv + 1); e += NT) {
         const int t = e / (kv + 1), c = e - t * (kv + 1);
@@ -685,14 +704,14 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
         for (int t = 0; t < jn; ++t) {
           const i64 i = j0 + t;
           if (own) X[t * nr + oc] = X[t * nr + oc] / LC[t * (kv + 1)];
-          __syncwarp();
+          wsync();
           if (cok) {
             const T xi = X[t * nr + cl];
             const int lim = (int)min((i64)kv, n - 1 - i);
             for (int c = 1 + r0; c <= lim; c += rstep)
               X[(t + c) * nr + cl] = fma(-LC[t * (kv + 1) + c], xi, X[(t + c) * nr + cl]);
           }
-          __syncwarp();
+          wsync();
         }
       }
       gsync();
@@ -707,7 +726,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     // holding rows base .. j1+kl; after the chunk, rows above j1-jn+1+kl are final.
     if (kl > 0 && n > 1) {
       i64 j1 = n - 2;
-      int jn = (int)min((i64)kChunk, j1 + 1);
+      int jn = (int)min((i64)kCh, j1 + 1);
       i64 base = j1 - jn + 1;
       load_rows(0, jn + kl, base);
       while (true) {
@@ -725,7 +744,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
             const int s0 = (int)(j - base);
             const int lm = (int)min((i64)kl, n - 1 - j);
             const T* lc = LC + t * kl;
-            if (kl <= 16) {  // sequential fma dot product, as reference dgemv 'T'
+            if (kl <= 16 || split) {  // sequential fma dot product, as reference dgemv 'T'
               if (own) {
                 T temp = T(0);
                 for (int i = 0; i < lm; ++i) temp = fma(X[(s0 + 1 + i) * nr + oc], lc[i], temp);
@@ -740,14 +759,14 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
                 if (lane == 0) X[s0 * nr + c] = fma(T(-1), temp, X[s0 * nr + c]);
               }
             }
-            __syncwarp();
+            wsync();
             const int l = (int)IP[t];
             if (l != s0 && own) {
               const T tv = X[l * nr + oc];
               X[l * nr + oc] = X[s0 * nr + oc];
               X[s0 * nr + oc] = tv;
             }
-            __syncwarp();
+            wsync();
           }
         }
         gsync();
@@ -759,7 +778,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
           gsync();
           break;
         }
-        const int jn2 = (int)min((i64)kChunk, nb + 1);
+        const int jn2 = (int)min((i64)kCh, nb + 1);
         // final rows: b rows > base + kl - 1 + ... = rows base + kl .. base + jn + kl - 1
         // become final only after the steps they can still be swapped with; steps of the
         // next chunk touch rows <= nb + kl = base - 1 + kl, so rows base + kl .. are final
@@ -779,10 +798,12 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
 // All nrhs right-hand sides, kMaxRhs per sweep.
 template <typename T, int G>
 __device__ void gbtrs_all(bool trans, i64 n, int kl, int ku, i64 nrhs, const T* __restrict__ ab, i64 ldab,
-                          const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem) {
+                          const i64* __restrict__ ipiv, T* __restrict__ b, i64 ldb, T* __restrict__ smem,
+                          int ch = kChunk) {
   if (n <= 0) return;
   for (i64 c0 = 0; c0 < nrhs; c0 += kMaxRhs)
-    gbtrs_group<T, G>(trans, n, kl, ku, (int)min((i64)kMaxRhs, nrhs - c0), ab, ldab, ipiv, b + c0 * ldb, ldb, smem);
+    gbtrs_group<T, G>(trans, n, kl, ku, (int)min((i64)kMaxRhs, nrhs - c0), ab, ldab, ipiv, b + c0 * ldb, ldb, smem,
+                      ch);
 }
 
 }  // namespace bm

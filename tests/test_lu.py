@@ -340,3 +340,32 @@ def test_cta_lu_panels_singular_and_rectangular(bm, gpu, orc, dt, m, n, l, u, ze
     got = F.factors.data.cpu().numpy()
     mask = orc.band_to_dense(np.ones_like(LU), m, l, l + u) != 0
     assert np.array_equal(orc.band_to_dense(got, m, l, l + u)[mask], orc.band_to_dense(LU, m, l, l + u)[mask])
+
+
+@pytest.mark.parametrize("dt,m,n,l,u,zero_cols", [(np.float64, 1500, 1500, 150, 150, ()),
+                                                  (np.float64, 700, 600, 140, 160, (33, 300)),
+                                                  (np.float32, 900, 900, 250, 240, (17,)),
+                                                  (np.float64, 600, 700, 200, 100, ())])
+def test_wide_band_panels_bitexact(bm, gpu, orc, dt, m, n, l, u, zero_cols):
+    """Bands whose one-column window exceeds shared memory go through the panel +
+    per-column replay launches: factors, pivots and info equal dgbtf2's bit for bit,
+    and square systems solve ('N' bit-exact, 'T' to 1e-12 / 1e-5)."""
+    rng = np.random.default_rng(m + n + l + u)
+    data = rng.standard_normal((l + u + 1, n)).astype(dt)
+    for c in zero_cols:
+        data[:, c] = 0.0
+    A = dev_band(bm, data, m, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(m, n, l, u, orc.lu_storage(data, n, l, u))
+    assert F.info == info
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+    got = F.factors.data.cpu().numpy()
+    mask = orc.band_to_dense(np.ones_like(LU), m, l, l + u) != 0
+    assert np.array_equal(orc.band_to_dense(got, m, l, l + u)[mask], orc.band_to_dense(LU, m, l, l + u)[mask])
+    if m == n and info == 0:
+        for nrhs in (1, 5):
+            b = rng.standard_normal((n, nrhs)).astype(dt)
+            bd = torch.from_numpy(b).to(gpu)
+            assert np.array_equal(F.solve(bd).cpu().numpy(), orc.gbtrs("N", n, l, u, LU, ipiv, b))
+            assert rel(F.T.solve(bd).cpu().numpy(), orc.gbtrs("T", n, l, u, LU, ipiv, b)) < \
+                (1e-12 if dt == np.float64 else 1e-5)
