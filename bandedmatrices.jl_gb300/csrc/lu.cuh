@@ -744,11 +744,26 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
             const int s0 = (int)(j - base);
             const int lm = (int)min((i64)kl, n - 1 - j);
             const T* lc = LC + t * kl;
-            if (kl <= 16 || split) {  // sequential fma dot product, as reference dgemv 'T'
+            if (kl <= 16) {  // sequential fma dot product, as reference dgemv 'T'
               if (own) {
                 T temp = T(0);
                 for (int i = 0; i < lm; ++i) temp = fma(X[(s0 + 1 + i) * nr + oc], lc[i], temp);
                 X[s0 * nr + oc] = fma(T(-1), temp, X[s0 * nr + oc]);
+              }
+            } else if (split) {  // group tree reduction per column (partials in the header)
+              for (int c = 0; c < nr; ++c) {
+                T temp = T(0);
+                for (int i = tid; i < lm; i += NT) temp = fma(X[(s0 + 1 + i) * nr + c], lc[i], temp);
+#pragma unroll
+                for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
+                if (lane == 0) smem[8 + wig] = temp;
+                Grp<G>::sync();
+                if (tid == 0) {
+                  T sum = smem[8];
+                  for (int w = 1; w < G; ++w) sum += smem[8 + w];
+                  X[s0 * nr + c] = fma(T(-1), sum, X[s0 * nr + c]);
+                }
+                Grp<G>::sync();
               }
             } else {  // warp tree reduction per column
               for (int c = cw0; c < cw0 + nw; ++c) {

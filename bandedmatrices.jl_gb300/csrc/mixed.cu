@@ -25,8 +25,10 @@ namespace bm {
 // coalesced read of the column), so no shared memory and no synchronisation are
 // needed.  Row i accumulates its terms in ascending column order.
 constexpr int kResRhs = 4;
-constexpr int kResQ = 5;  // window rows 32*kResQ >= 32 + kl + ku  (kl + ku <= 128)
+constexpr int kResQ = 5;      // window rows 32*Q >= 32 + kl + ku: Q = 5 for kl + ku <= 128,
+constexpr int kResQWide = 9;  // Q = 9 for kl + ku <= 256 (chosen per launch)
 
+template <int kResQ>
 __device__ void residual_rows(i64 n, i64 rb, i64 re, int kl, int ku, int nr, const double* __restrict__ band,
                               i64 ldab, const double* __restrict__ B, const double* __restrict__ X, i64 ld,
                               float* __restrict__ R32, bool want_anorm, double& anorm, double* rnorm,
@@ -123,8 +125,9 @@ struct MixedParams {
   i64 group_elems;   // shared-memory floats per group
 };
 
-// One system of the batch (index s) by a group of G warps in `smem`.
-template <int G>
+// One system of the batch (index s) by a group of G warps in `smem`; Q sizes the
+// residual's register window.
+template <int G, int Q>
 __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
   constexpr int NT = Grp<G>::NT;
   const int tid = Grp<G>::tid(), wig = tid >> 5;
@@ -192,7 +195,7 @@ __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
         for (;;) {
           double rnorm[kResRhs], xnorm[kResRhs], an = 0.0;
           const bool first = anorm < 0.0;
-          residual_rows(n, rb, re, kl, ku, nr, A + kl, ldab, Bc, Xc, d.ldb, Rc, first, an, rnorm, xnorm);
+          residual_rows<Q>(n, rb, re, kl, ku, nr, A + kl, ldab, Bc, Xc, d.ldb, Rc, first, an, rnorm, xnorm);
           if (first) anorm = grp_max<G>(an, red);
           be = 0.0;
           for (int c = 0; c < kResRhs; ++c) {
@@ -227,7 +230,7 @@ __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
 
 // Two-part schedule, as gbsv_batched_kernel: wide systems (order[0..n_wide)) one per
 // CTA of W warps, then narrow systems one per warp in group_elems-float slices.
-template <int W>
+template <int W, int Q>
 __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParams p, i64 n_wide) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* base = reinterpret_cast<float*>(smem_raw);
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
   for (;;) {
     idx = next_item<W>(p.counter, reinterpret_cast<int*>(base));
     if (idx >= n_wide) break;
-    dsgbsv_system<W>(p, p.order ? p.order[idx] : idx, base);
+    dsgbsv_system<W, Q>(p, p.order ? p.order[idx] : idx, base);
     __syncthreads();
   }
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
       my = __shfl_sync(0xffffffffu, v, 0);
     }
     if (my >= p.count) break;
-    dsgbsv_system<1>(p, p.order ? p.order[my] : my, ws);
+    dsgbsv_system<1, Q>(p, p.order ? p.order[my] : my, ws);
     my = -1;
   }
 }
@@ -257,19 +260,19 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
 // FP32 solve chunk, FP64 residual scratch; 0 when the refined solve does not support
 // the band (kl + ku above the residual window).
 static i64 mixed_group_elems(i64 kl, i64 ku, bool wide) {
-  if (kl + ku + 32 > 32 * kResQ) return 0;
+  if (kl + ku + 32 > 32 * kResQWide) return 0;
   (void)wide;
   const i64 fac = gbtrf_smem_elems<4>((int)kl, (int)ku);
   const i64 f = std::max(std::max(fac, gbtrs_smem_elems((int)kl, (int)ku)), (i64)(kHdr + 16));
   return ((f + 3) / 4) * 4;
 }
 
-template <int W>
+template <int W, int Q>
 static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
   const i64 we = sc.n_wide > 0 ? mixed_group_elems(sc.wide_kl, sc.wide_ku, true) : 1;
   const i64 ne = sc.n_wide < p.count ? mixed_group_elems(sc.narrow_kl, sc.narrow_ku, false) : 1;
   if (we == 0 || ne == 0) {
-    set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQ - 32);
+    set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQWide - 32);
     return BM_ERR_UNSUPPORTED;
   }
   p.group_elems = sc.n_wide < p.count ? ne : 0;
@@ -278,11 +281,11 @@ static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t s
     set_error("%s: the schedule's shared memory (%lld bytes) exceeds the per-CTA limit", name, (long long)bytes);
     return BM_ERR_UNSUPPORTED;
   }
-  const void* kfn = (const void*)dsgbsv_batched_kernel<W>;
+  const void* kfn = (const void*)dsgbsv_batched_kernel<W, Q>;
   int r = cuda_status(ensure_smem(kfn, (int)bytes), name);
   if (r) return r;
   int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsgbsv_batched_kernel<W>, 32 * W, (int)bytes),
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsgbsv_batched_kernel<W, Q>, 32 * W, (int)bytes),
                   name);
   if (r) return r;
   per_sm = std::max(per_sm, 1);
@@ -290,7 +293,7 @@ static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t s
   const i64 grid = std::min<i64>((i64)num_sms() * per_sm, std::max<i64>(need, 1));
   r = cuda_status(cudaMemsetAsync(p.counter, 0, sizeof(int32_t), stream), name);
   if (r) return r;
-  dsgbsv_batched_kernel<W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(p, sc.n_wide);
+  dsgbsv_batched_kernel<W, Q><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(p, sc.n_wide);
   return launch_status(name);
 }
 
@@ -304,8 +307,12 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
   if (!(p.tol >= 0.0)) return -15;
   if (p.maxit < 0) return -16;
   if (p.count == 0) return BM_OK;
-  if (sc->warps == 8) return dsgbsv_launch<8>(p, *sc, stream, name);
-  return dsgbsv_launch<4>(p, *sc, stream, name);
+  const i64 kvmax = std::max(sc->n_wide > 0 ? sc->wide_kl + sc->wide_ku : 0,
+                             sc->n_wide < p.count ? sc->narrow_kl + sc->narrow_ku : 0);
+  const bool wideq = kvmax + 32 > 32 * kResQ;
+  if (sc->warps == 8) return wideq ? dsgbsv_launch<8, kResQWide>(p, *sc, stream, name)
+                                   : dsgbsv_launch<8, kResQ>(p, *sc, stream, name);
+  return wideq ? dsgbsv_launch<4, kResQWide>(p, *sc, stream, name) : dsgbsv_launch<4, kResQ>(p, *sc, stream, name);
 }
 
 }  // namespace bm

@@ -54,6 +54,34 @@ class BandedLU:
         """F \\ B (copies B)."""
         return ldiv_(self, B.clone())
 
+    def inv_norm1_estimate(self, maxit: int = 5) -> float:
+        """Estimate of ||A^{-1}||_1 from the factors, the quantity LAPACK's xGBCON
+        estimates with xLACN2: Hager's method with Higham's refinements (sign vector,
+        stop when the gradient does not grow), two triangular-solve pairs per iteration
+        on the device."""
+        n = self.shape[0]
+        dev, dt = self.factors.data.device, self.factors.data.dtype
+        x = torch.full((n,), 1.0 / n, dtype=dt, device=dev)
+        est, last_j = 0.0, -1
+        for it in range(maxit):
+            y = self.solve(x)
+            new = float(y.abs().sum())
+            if it > 0 and new <= est:
+                break
+            est = new
+            z = TransposedBandedLU(self).solve(torch.where(y >= 0, 1.0, -1.0).to(dt))
+            j = int(z.abs().argmax())
+            if it > 0 and (j == last_j or float(z.abs().max()) <= float((z * x).sum())):
+                break
+            last_j = j
+            x = torch.zeros(n, dtype=dt, device=dev)
+            x[j] = 1.0
+        # Higham's alternative estimate (the alternating-sign vector)
+        alt = torch.arange(n, dtype=dt, device=dev)
+        alt = (1.0 + alt / max(n - 1, 1)) * torch.where(alt.remainder(2) == 0, 1.0, -1.0).to(dt)
+        est2 = 2.0 * float(self.solve(alt).abs().sum()) / (3.0 * n)
+        return max(est, est2)
+
     # -- L, U, p, P (BandedLU.jl:114-130): dense host-side views for inspection/tests
     @property
     def p(self) -> np.ndarray:

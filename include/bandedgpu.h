@@ -215,7 +215,7 @@ int bm_sgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t
  * final backward error per system (max over its right-hand sides), info the FP32
  * factorization's info.  R32 is FP32 workspace laid out like B but with leading
  * dimension n (n*nrhs floats per system at its b_offset); counter is one int32 of
- * workspace.  kl + ku <= 128 per system.  No counterpart in the
+ * workspace.  kl + ku <= 256 per system.  No counterpart in the
  * reference; per system it replaces lu! + ldiv! (src/banded/BandedLU.jl:90-103,
  * src/banded/linalg.jl:24-30) when the caller accepts a backward-error target. */
 int bm_dsgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const double *AB,
