@@ -17,6 +17,7 @@ from .lu import BandedLU, ldiv_, lu, lu_, transpose
 from .batched import BandedBatch, lpt_order
 from .qr import BandedQR, lmul_, qr
 from .autograd import BandedSolve, banded_solve
+from .refine import solve_refined
 from . import pde
 
 __all__ = [
@@ -24,6 +25,7 @@ __all__ = [
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
+    "solve_refined",
     "BandedSolve", "banded_solve",
 ]
 

@@ -457,6 +457,8 @@ def run_batched(bm, dev, stream):
         batch.B.copy_(B0)
 
     restore()
+    tune_plain = batch.tune("plain")  # autotuner: schedule for the plain solve
+    restore()
     batch.factor_solve()  # warm-up (device set-up)
     t_plain = _timed(batch.factor_solve, stream, reps=2, restore=restore)
     # backward error of the plain solutions on a sample of systems (FP64 residual on the GPU)
@@ -475,6 +477,7 @@ def run_batched(bm, dev, stream):
             be = r.abs().max().item() / (an * X[:, c].abs().max().item() + Bs[:, c].abs().max().item())
             berr_plain = max(berr_plain, be)
     restore()
+    tune_mixed = batch.tune("mixed", tol=1e-10, maxit=30)
     batch.solve_mixed(1e-10, 30)
     t_mixed = _timed(lambda: batch.solve_mixed(1e-10, 30), stream, reps=2)
     its = batch.iters.cpu().numpy()
@@ -488,7 +491,44 @@ def run_batched(bm, dev, stream):
                                     "iters_max": int(its.max()), "iters_mean": float(its.mean())},
         "speedup_mixed_vs_plain": t_plain / t_mixed,
         "launches_per_solve": 1,
+        "schedule": {"plain": {k: tune_plain[k] for k in ("warps", "narrow_cols", "ms", "tune_s")},
+                     "mixed": {k: tune_mixed[k] for k in ("warps", "narrow_cols", "ms", "tune_s")},
+                     "candidates_timed": len(tune_plain["candidates"]) + len(tune_mixed["candidates"])},
     }
+
+
+def run_refined(bm, dev, stream):
+    """One system n = 2^20, l = u = 128: randn band + 16 on the diagonal (kappa_1 ~ 1e6,
+    estimated from the LU factors at n = 2^16 with the same recipe), b randn.  Float32
+    LU + Float64-residual refinement to 1e-10 against the plain Float64 LU solve."""
+    import torch
+
+    def band(n, seed):
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        A = bm.BandedMatrix(bm.band_storage(257, n, torch.float64, dev), n, 128, 128)
+        A.data.normal_(generator=g)
+        A.data[128] += 16.0
+        return A, torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+
+    Ap, _ = band(1 << 16, 20)
+    Fp = bm.lu(Ap)
+    kappa = float(Ap.data.abs().sum(0).max()) * Fp.inv_norm1_estimate()
+    del Ap, Fp
+    A, b = band(1 << 20, 21)
+    out = {}
+    t_ref = _timed(lambda: out.__setitem__("r", bm.solve_refined(A, b, tol=1e-10)), stream)
+    x, st = out["r"]
+    t_plain = _timed(lambda: out.__setitem__("p", bm.lu(A).solve(b)), stream)
+    xp = out["p"]
+    r = b.clone()
+    bm.mul_(r, A, xp, -1.0, 1.0)
+    an = float(A.data.abs().sum(0).max())
+    berr_plain = float(r.abs().max()) / (an * float(xp.abs().max()) + float(b.abs().max()))
+    del A, b, x, xp, r
+    return {"workload": "n=2^20, l=u=128, f64 randn + 16 I (kappa_1 ~ %.1e at n=2^16), b randn" % kappa,
+            "refined_ms": t_ref, "iters": st["iters"], "berr": st["berr"], "plain_fp64_ms": t_plain,
+            "berr_plain": berr_plain, "speedup_refined_vs_plain": t_plain / t_ref}
 
 
 def run_cpu_runnable(bm, dev, stream):
@@ -539,7 +579,7 @@ def run_qr(bm, dev, stream):
             "gflops_factor": 4.0 * n * (l + 1) * (2 * l + u) / (t_f / 1e3) / 1e9, "berr": berr}
 
 
-def run_pde(bm, dev, stream, G=96):
+def run_pde(bm, dev, stream, G=512):
     """Differentiated PDE solve: 5-point variable-coefficient diffusion on a G x G grid,
     x = A \\ b, L = w.x, adjoint dL/db and dL/dA; directional central difference h = 1e-6."""
     import numpy as np
@@ -702,6 +742,8 @@ def main():
         torch.cuda.empty_cache()
         out["cpu_runnable"] = run_cpu_runnable(bm, dev, stream)
         out["qr_least_squares"] = run_qr(bm, dev, stream)
+        torch.cuda.empty_cache()
+        out["refined_single"] = run_refined(bm, dev, stream)
         torch.cuda.empty_cache()
         out["pde_adjoint"] = run_pde(bm, dev, stream)
     if rank == 0:

@@ -96,3 +96,27 @@ def test_mixed_matches_fp64_systems_and_iterations(bm, gpu, orc):
     torch.cuda.synchronize()
     assert batch.berr.max().item() <= 1e-12
     assert batch.iters.max().item() <= 6
+
+
+def test_single_system_refined_wide_and_conditioned(bm, gpu, orc):
+    """solve_refined (Float32 LU, Float64 residuals) on a band whose Float64 window is
+    too wide for one CTA and a shift giving kappa ~ 1e5..1e6: the backward error
+    reaches 1e-10, and the solution matches the Float64 LU solve to kappa * 1e-10."""
+    n, kl, ku = 4000, 130, 120
+    g = torch.Generator(device=gpu)
+    g.manual_seed(31)
+    A = bm.BandedMatrix(bm.band_storage(kl + ku + 1, n, torch.float64, gpu), n, kl, ku)
+    A.data.normal_(generator=g)
+    A.data[ku] += 16.0
+    b = torch.randn(n, dtype=torch.float64, device=gpu, generator=g)
+    x, st = bm.solve_refined(A, b, tol=1e-10)
+    assert st["info"] == 0 and st["berr"] <= 1e-10 and st["iters"] >= 1
+    F = bm.lu(A)
+    x64 = F.solve(b)
+    kappa = float(A.data.abs().sum(0).max()) * F.inv_norm1_estimate()
+    assert 1e3 < kappa < 1e8, kappa
+    assert float((x - x64).abs().max()) <= 10 * kappa * 1e-10 * float(x64.abs().max())
+    r = b.clone()
+    bm.mul_(r, A, x, -1.0, 1.0)
+    anorm = float(A.data.abs().sum(0).max())
+    assert float(r.abs().max()) / (anorm * float(x.abs().max()) + float(b.abs().max())) <= 1.5e-10
