@@ -199,6 +199,66 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- GPU
+def cpu_lu_baselines():
+    """The reference's CPU path for the LU/QR/PDE workloads on the host cores: OpenBLAS
+    dgbtrf + dgbtrs through SciPy (the LAPACK routines lu!/ldiv! ccall; Julia absent),
+    all OpenBLAS threads, seeded NumPy inputs of the same shapes; bounded samples are
+    scaled by their share of the work and say so.  QR: the _banded_qr! restatement in C
+    (one thread, as the reference's Julia loop)."""
+    import numpy as np
+    from scipy.linalg import lapack
+
+    L = _openblas()
+    threads = int(L.scipy_openblas_get_num_threads())
+    rng = np.random.default_rng(7)
+
+    def gb(n, kl, ku, shift):
+        ab = np.zeros((2 * kl + ku + 1, n), order="F")
+        ab[kl:, :] = rng.standard_normal((kl + ku + 1, n))
+        ab[kl + ku, :] += shift
+        return ab
+
+    def lu_solve(n, kl, ku, shift, nrhs=1, trans=0):
+        ab = gb(n, kl, ku, shift)
+        b = rng.standard_normal((n, nrhs))
+        t0 = time.perf_counter()
+        lub, piv, info = lapack.dgbtrf(ab, kl, ku, overwrite_ab=1)
+        t1 = time.perf_counter()
+        x, info2 = lapack.dgbtrs(lub, kl, ku, b, piv, trans=trans)
+        t2 = time.perf_counter()
+        return t1 - t0, t2 - t1
+
+    out = {"threads": threads, "kind": "reference", "impl": "OpenBLAS dgbtrf/dgbtrs via SciPy (stand-in for Julia's ccall)"}
+    f, s_ = lu_solve(10000, 4, 3, 10.0)
+    out["config1_lu_solve_ms"] = (f + s_) * 1e3
+    # 4096 uneven systems: a sample of 512 of them, scaled by its share of the flops
+    n, kl, ku, nrhs = batched_config()
+    idx = np.random.default_rng(1).choice(len(n), 512, replace=False)
+    cost = n * (2 * kl * (kl + ku) + kl) + nrhs * 2 * n * (2 * kl + ku + 1)
+    tot = 0.0
+    for s in idx:
+        f, s_ = lu_solve(int(n[s]), int(kl[s]), int(ku[s]), 2.0 * (kl[s] + ku[s]), int(nrhs[s]))
+        tot += f + s_
+    t_all = tot * cost.sum() / cost[idx].sum()
+    out["batched_4096_ms"] = t_all * 1e3
+    out["batched_systems_per_s"] = len(n) / t_all
+    out["batched_sample"] = "512 of the 4096 systems (seeded), time scaled by the flop share"
+    f, s_ = lu_solve(1 << 20, 128, 128, 16.0)
+    out["refined_config_fp64_lu_solve_ms"] = (f + s_) * 1e3
+    f, s_ = lu_solve(262144, 512, 512, 4.0 * 1024, trans=0)
+    out["pde_factor_ms"], out["pde_solve_ms"] = f * 1e3, s_ * 1e3
+    import oracle  # CPU-baseline leg: the _banded_qr! restatement
+
+    nq, lq = 1 << 15, 32
+    D = np.zeros((3 * lq + 1, nq), order="F")
+    D[lq:, :] = rng.standard_normal((2 * lq + 1, nq))
+    t0 = time.perf_counter()
+    oracle.gbqrf(nq, nq, lq, 2 * lq, D)
+    out["qr_factor_n2e18_ms"] = (time.perf_counter() - t0) * 1e3 * (1 << 18) / nq
+    out["qr_sample"] = "n = 2^15, l = u = 32, scaled by columns to n = 2^18"
+    return out
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -748,6 +808,8 @@ def main():
         out["pde_adjoint"] = run_pde(bm, dev, stream)
     if rank == 0:
         if not args.no_cpu_baseline:
+            if not args.sweep_only:
+                out["cpu_baseline_solvers"] = cpu_lu_baselines()
             cb = cpu_sweep(1, 1)
             out["cpu_baseline"] = {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
                                    "sample": cb["sample"], "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"]}
