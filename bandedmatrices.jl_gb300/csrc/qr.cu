@@ -195,20 +195,34 @@ __global__ void __launch_bounds__(32 * G) gbqrf_kernel(i64 m, i64 n, int l, int 
 template <typename T>
 __global__ void gbqr_lmul_kernel(bool adjoint, i64 m, i64 n, int l, int u, const T* __restrict__ D, i64 ldd,
                                  const T* __restrict__ tau, i64 ntau, i64 nrhs, T* __restrict__ B, i64 ldb) {
-  const i64 c = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nrhs) return;
-  T* b = B + c * ldb;
+  // four threads per right-hand side: thread q takes rows k+1+q, k+5+q, ... of each
+  // reflector, so the dot product has the four interleaved partial sums of gbqrf's
+  // reflector application, combined (s0+s1)+(s2+s3) by two butterfly shuffles
+  const i64 c = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int q = threadIdx.x & 3;
+  const bool live = c < nrhs;
+  T* b = B + (live ? c : 0) * ldb;
   const i64 kmax = min(min(m, n), ntau);
   const int ilo = max(1, -u);
   for (i64 t = 0; t < kmax; ++t) {
     const i64 k = adjoint ? t : kmax - 1 - t;
     const T* d = D + (u - k) + k * ldd;  // d[i] = D[(i - k + u), k]
     const i64 ihi = min(k + l, m - 1);
-    T v = b[k];
-    for (i64 i = k + ilo; i <= ihi; ++i) v = fma(d[i], b[i], v);
-    v = tau[k] * v;
-    b[k] = b[k] - v;
-    for (i64 i = k + ilo; i <= ihi; ++i) b[i] = fma(-d[i], v, b[i]);
+    T part = T(0);
+    if (live)
+      for (i64 i = k + 1 + q; i <= ihi; i += 4)
+        if (i >= k + ilo) part = fma(d[i], b[i], part);
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    if (live) {
+      const T bk = b[k];
+      const T v = tau[k] * (bk + part);
+      for (i64 i = k + 1 + q; i <= ihi; i += 4)
+        if (i >= k + ilo) b[i] = fma(-d[i], v, b[i]);
+      __syncwarp(0xfu << (threadIdx.x & 28));  // the group's reads of b[k] precede the store
+      if (q == 0) b[k] = bk - v;
+    }
+    __syncwarp();
   }
 }
 
@@ -261,9 +275,9 @@ static int gbqr_lmul_impl(char trans, i64 m, i64 n, i64 l, i64 u, const T* D, i6
   if (nrhs < 0) return -10;
   if (ldb < std::max<i64>(1, m)) return -12;
   if (m == 0 || nrhs == 0 || ntau == 0) return BM_OK;
-  const int threads = (int)std::min<i64>(nrhs, 128);
-  gbqr_lmul_kernel<T><<<(unsigned)ceil_div(nrhs, threads), threads, 0, stream>>>(adj, m, n, (int)l, (int)u, D, ldd,
-                                                                                  tau, ntau, nrhs, B, ldb);
+  const int threads = nrhs <= 8 ? 32 : 128;  // whole warps: four lanes per right-hand side
+  gbqr_lmul_kernel<T><<<(unsigned)ceil_div(4 * nrhs, threads), threads, 0, stream>>>(adj, m, n, (int)l, (int)u, D,
+                                                                                      ldd, tau, ntau, nrhs, B, ldb);
   return launch_status(name);
 }
 

@@ -386,10 +386,13 @@ int P##gbqr_lmul(char trans, i64 m, i64 n, i64 l, i64 u, const T *D, i64 ldd, co
         T *bj = B + r * ldb;                                                                    \
         for (i64 t = 0; t < kmax; t++) {                                                        \
             i64 k = adj ? t : kmax - 1 - t;                                                     \
-            T v = bj[k];                                                                        \
+            /* bj[k] + the reflector's dot product in four interleaved partial sums  */ \
+            /* (rows k+1+t, k+5+t, ...), combined (s0+s1)+(s2+s3): reflectorApply!'s  */ \
+            /* dot, in the order the factorization (gbqrf) uses                        */ \
+            T s4[4] = {0, 0, 0, 0};                                                             \
             for (i64 i = k + ilo; i <= imin(k + l, m - 1); i++)                                 \
-                v = FMA(D[(i - k + u) + k * ldd], bj[i], v);                                    \
-            v = tau[k] * v;                                                                     \
+                s4[(i - k - 1) & 3] = FMA(D[(i - k + u) + k * ldd], bj[i], s4[(i - k - 1) & 3]); \
+            T v = tau[k] * (bj[k] + ((s4[0] + s4[1]) + (s4[2] + s4[3])));                       \
             bj[k] = bj[k] - v;                                                                  \
             for (i64 i = k + ilo; i <= imin(k + l, m - 1); i++)                                 \
                 bj[i] = FMA(-D[(i - k + u) + k * ldd], v, bj[i]);                               \
