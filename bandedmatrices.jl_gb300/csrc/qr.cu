@@ -250,7 +250,11 @@ static int gbqrf_impl(i64 m, i64 n, i64 l, i64 u, T* D, i64 ldd, T* tau, cudaStr
     set_error("%s: band (l=%lld, u=%lld) exceeds the window limit", name, (long long)l, (long long)u);
     return BM_ERR_UNSUPPORTED;
   }
-  if ((l + 1) * (u + 1) >= 512) {
+  if (u >= 48) {  // four threads per following column: 8 warps cover 64 columns per pass
+    int r = cuda_status(ensure_smem((const void*)gbqrf_kernel<T, 8>, (int)bytes), name);
+    if (r) return r;
+    gbqrf_kernel<T, 8><<<1, 256, (int)bytes, stream>>>(m, n, (int)l, (int)u, D, ldd, tau);
+  } else if ((l + 1) * (u + 1) >= 512) {
     int r = cuda_status(ensure_smem((const void*)gbqrf_kernel<T, 4>, (int)bytes), name);
     if (r) return r;
     gbqrf_kernel<T, 4><<<1, 128, (int)bytes, stream>>>(m, n, (int)l, (int)u, D, ldd, tau);
