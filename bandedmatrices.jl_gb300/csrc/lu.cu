@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, 
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
   T* P = reinterpret_cast<T*>(smem_raw);  // panel: column c (0..jb-1) x row r (matrix row j0 + r)
-  int* hdr = reinterpret_cast<int*>(P + (i64)RS * NB);
+  int* hdr = reinterpret_cast<int*>(P + (i64)RS * NB);  // [0] pivot, [4..] per-warp keys and indices
   // entry (row j0+r, column j0+c) of the storage when it lies in it
   auto sidx = [&](int r, int c) -> i64 {
     const i64 i = j0 + r, col = j0 + c;
@@ -93,20 +93,38 @@ __global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, 
     const i64 gj = j0 + c;
     const int km = (int)min((i64)kl, m - 1 - gj);
     T* colc = P + c * RS;
-    if (wig == 0) {
+    {  // idamax over rows c..c+km: every warp scans rows r = tid, tid+NT, ..., then the
+       // warps' (key, first index) pairs are combined (larger key, else smaller index)
       unsigned long long key = 0ull;
       int idx = 0x7fffffff;
-      for (int r = lane; r <= km; r += 32) {
+      for (int r = tid; r <= km; r += NT) {
         const unsigned long long k = pivot_key(colc[c + r], r == 0);
         if (idx == 0x7fffffff || k > key) {
           key = k;
           idx = r;
         }
       }
-      const int jp = warp_argmax_first(key, idx);
+      const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+      const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+      const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+      const int widx = (int)__reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? (unsigned)idx : 0x7fffffffu);
+      unsigned long long* wk = reinterpret_cast<unsigned long long*>(hdr + 4);  // 8 keys
+      int* wi = hdr + 4 + 2 * (NT / 32);                                         // 8 indices
       if (lane == 0) {
-        hdr[0] = jp;
-        ipiv[gj] = gj + jp + 1;
+        wk[wig] = ((unsigned long long)mhi << 32) | mlo;
+        wi[wig] = widx;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        unsigned long long bk = wk[0];
+        int bi = wi[0];
+        for (int w = 1; w < NT / 32; ++w)
+          if (wi[w] != 0x7fffffff && (bi == 0x7fffffff || wk[w] > bk || (wk[w] == bk && wi[w] < bi))) {
+            bk = wk[w];
+            bi = wi[w];
+          }
+        hdr[0] = bi;
+        ipiv[gj] = gj + bi + 1;
       }
     }
     __syncthreads();
@@ -128,13 +146,14 @@ __global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, 
       inf = gj + 1;
     }
     __syncthreads();
-    if (nonsingular) {
-      const int nc = jb - 1 - c;
-      for (int e = tid; e < km * nc; e += NT) {
-        const int cc = c + 1 + e / km, r = c + 1 + e % km;
-        T* col = P + cc * RS;
-        const T u = col[c];
-        if (is_nonzero(u)) col[r] = fma(colc[r], -u, col[r]);
+    if (nonsingular) {  // rank-1 update of the panel's later columns: a thread per row
+      for (int r = c + 1 + tid; r <= c + km; r += NT) {
+        const T l = colc[r];
+        for (int cc = c + 1; cc < jb; ++cc) {
+          T* col = P + cc * RS;
+          const T u = col[c];
+          if (is_nonzero(u)) col[r] = fma(l, -u, col[r]);
+        }
       }
     }
     __syncthreads();
@@ -198,7 +217,19 @@ __global__ void __launch_bounds__(32 * kWideWarps) gbtrf_replay_kernel(i64 m, i6
         const int km = (int)min((i64)kl, m - 1 - (j0 + k));
         const T nu = -u;
         const T* lk = L + k * RS;
-        for (int r = k + 1 + lane; r <= k + km; r += 32) colbuf[r] = fma(lk[r], nu, colbuf[r]);
+        // rows k+1+lane, +32, ...: eight loads issued before their fmas
+        int r = k + 1 + lane;
+        for (; r + 7 * 32 <= k + km; r += 8 * 32) {
+          T lv[8], av[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            lv[q] = lk[r + 32 * q];
+            av[q] = colbuf[r + 32 * q];
+          }
+#pragma unroll
+          for (int q = 0; q < 8; ++q) colbuf[r + 32 * q] = fma(lv[q], nu, av[q]);
+        }
+        for (; r <= k + km; r += 32) colbuf[r] = fma(lk[r], nu, colbuf[r]);
       }
       __syncwarp();
     }
@@ -214,7 +245,7 @@ template <typename T>
 static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
                            const char* name) {
   const int R = (int)kl + kNB, RS = R | 1;
-  const i64 pbytes = ((i64)RS * kNB + 16) * (i64)sizeof(T);
+  const i64 pbytes = (i64)RS * kNB * (i64)sizeof(T) + 256;  // panel + header (pivot, 8 warp keys/indices)
   const i64 rbytes = ((i64)RS * kNB + (i64)RS * kWideWarps) * (i64)sizeof(T);
   if (pbytes > 227 * 1024 || rbytes > 227 * 1024) {
     set_error("%s: band (kl=%lld) exceeds the panel limit", name, (long long)kl);
