@@ -18,7 +18,7 @@ from .batched import BandedBatch, lpt_order
 from .qr import BandedQR, lmul_, qr
 from .autograd import BandedSolve, banded_solve
 from .refine import solve_refined
-from . import pde
+from . import pde, shard
 
 __all__ = [
     "BandedGPUError", "BandedMatrix", "BandError", "DimensionMismatch", "band_storage", "bandeddata",
