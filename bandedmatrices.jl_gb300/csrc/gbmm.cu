@@ -9,11 +9,15 @@
 // max(0,k-Al,j-Bu) <= v <= min(nu-1,k+Au,j+Bl).  Bands of C outside (Al+Bl, Au+Bu) are
 // scaled by beta (set to zero when beta == 0, C not read), as gbmm! does (:286-288).
 //
-// Structure: a persistent kernel, tiles of TJ consecutive C columns.  Per tile, thread 0
-// streams A's columns [j0-Bu, j0+TJ+Bl), B's columns [j0, j0+TJ) and (beta != 0) C's
-// columns into a two-slot shared-memory ring with 1-D TMA bulk copies (mbarrier
-// completion).  A warp owns one C column at a time; lane r holds C storage rows
-// r, r+32, r+64, ... in registers, so B(v,j) is one broadcast shared load per term.
+// Three paths, all in that order:
+//   * interior column tiles with beta == 0 and bands of at most 33 rows take a
+//     register-blocked kernel: gbmm_f32x2_kernel (Float32: TMA bulk tiles, packed fma
+//     pairs) or gbmm_reg_kernel (Float64, or Float32 with an even lda);
+//   * the edge columns of those shapes take gbmm_simple_kernel (a thread per entry);
+//   * everything else takes gbmm_tma_kernel: a persistent kernel over tiles of TJ C
+//     columns, whose thread 0 streams A's columns [j0-Bu, j0+TJ+Bl), B's columns and
+//     (beta != 0) C's columns into a two-slot ring with 1-D TMA bulk copies, a warp per
+//     C column and its lanes over the column's storage rows.
 // Roofline: HBM for Float32; the FP64 pipe for Float64 on GB300 (about 2 flop/byte).
 #include <cstdio>
 #include <cstdlib>

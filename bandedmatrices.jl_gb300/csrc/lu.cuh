@@ -8,17 +8,24 @@
 // (logical row r <-> physical (j+r) mod (kl+1), logical column c <-> (j+c) mod
 // (kl+ku+1)), so the window slides one row and one column per step without moving
 // data.  The row that enters at each step is fetched P steps ahead with cp.async
-// into a staging ring.  The arithmetic is LAPACK's dgbtf2 operation for operation:
-// idamax (first index of the largest |a|), row interchange over columns j..ju,
-// scaling by the reciprocal of the pivot, and the rank-1 update a <- fma(l_i, -u_c, a)
-// skipping u_c == 0 -- so factors and pivots equal the oracle's bit for bit.
+// into a staging ring.  Each thread owns whole window columns; a step is two group
+// barriers (column 0's multipliers, then every column's interchange, update and slide,
+// with the next pivot found by the owner of the next column).  The arithmetic is
+// LAPACK's dgbtf2 operation for operation: idamax (first index of the largest |a|), row
+// interchange, scaling by the reciprocal of the pivot, and the rank-1 update
+// a <- fma(l_i, -u_c, a) skipping u_c == 0 -- so factors and pivots equal the oracle's
+// bit for bit.  A panel form (gbtrf_blocked_group; and, across the GPU for bands whose
+// window exceeds shared memory, lu.cu's panel + replay kernels) keeps the same
+// per-element sequence.
 //
-// gbtrs: the sweeps are sequential in j; each step's update is spread over the
-// group's threads, up to kMaxRhs right-hand sides at once, and b is staged through
-// shared memory in chunks of kChunk steps.  Every element receives its updates in
-// the same order as in dgbtrs/dtbsv (the transposed triangular solve is done in axpy
-// form, which preserves each element's accumulation order).  Only the L^T dot
-// products of the transposed solve use a tree reduction when kl > 16.
+// gbtrs: the sweeps are sequential in j and run in chunks of up to kChunk steps: the
+// group stages a chunk's L or U columns, pivots and rows of b through shared memory,
+// then each warp sweeps its own right-hand sides with warp-level synchronisation (or,
+// for few right-hand sides on a wide band, the whole group shares each column's rows).
+// Every element receives its updates in the same order as in dgbtrs/dtbsv (the
+// transposed triangular solve is done in axpy form, which preserves each element's
+// accumulation order).  Only the L^T dot products of the transposed solve use a tree
+// reduction when kl > 16.
 #pragma once
 #include "common.cuh"
 
