@@ -6,6 +6,7 @@
 #include <mutex>
 
 #include "lu.cuh"
+#include "lureg.cuh"
 
 namespace bm {
 
@@ -342,6 +343,8 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
   if (!info) return -8;
   if (m == 0 || n == 0) return cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
   if (!ipiv) return -7;
+  // bands whose window fits the register file: one lane per window column
+  if (reg_class<T>(kl, ku)) return gbtrf_reg_run<T>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
   const i64 bytes = gbtrf_smem_elems<kP>((int)kl, (int)ku) * (i64)sizeof(T);
   const i64 bbytes = gbtrf_blocked_smem_elems<T>((int)kl, (int)ku) * (i64)sizeof(T);
   // the one-column step where its window fits (measured faster); panels of kNB
