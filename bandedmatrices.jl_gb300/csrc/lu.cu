@@ -284,10 +284,22 @@ template <typename T, int G>
 __device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i64* ipiv, T* B, i64* info, T* smem) {
   T* ab = AB + d.ab_offset;
   i64* ip = ipiv + d.ipiv_offset;
-  const i64 r = gbtrf_group<T, kP, G>(d.n, d.n, (int)d.kl, (int)d.ku, ab, d.ldab, ip, smem);
-  if (Grp<G>::tid() == 0) info[s] = r;
+  const int kl = (int)d.kl, ku = (int)d.ku, tid = Grp<G>::tid();
+  // the register window where the band fits the group; its solve sweeps for Float32
+  // (for Float64 the staged sweeps keep more of the FP64 pipe busy)
+  const i64 r = reg_fits<T>(kl, ku, 32 * G)
+                    ? gbtrf_reg_any<T, 32 * G>(d.n, d.n, kl, ku, ab, d.ldab, ip, smem, tid, 32 * G, G > 1)
+                    : gbtrf_group<T, kP, G>(d.n, d.n, kl, ku, ab, d.ldab, ip, smem);
+  if (tid == 0) info[s] = r;
   Grp<G>::sync();
-  if (r == 0) gbtrs_all<T, G>(false, d.n, (int)d.kl, (int)d.ku, d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem);
+  if (r == 0) {
+    if (sizeof(T) == 4 && reg_solve_fits<T>(kl, ku)) {
+      if ((tid >> 5) == 0)
+        gbtrs_reg_any<T, kMaxRhs>(d.n, kl, ku, (int)d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem, tid & 31);
+    } else {
+      gbtrs_all<T, G>(false, d.n, kl, ku, d.nrhs, ab, d.ldab, ip, B + d.b_offset, d.ldb, smem);
+    }
+  }
   Grp<G>::sync();
 }
 
@@ -390,6 +402,9 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
   if (ldab < 2 * kl + ku + 1) return -7;
   if (ldb < std::max<i64>(1, n)) return -10;
   if (n == 0 || nrhs == 0) return BM_OK;
+  // the register-window sweeps (one warp per 32 right-hand sides) where the band fits
+  if (notr && sizeof(T) == 4 && reg_solve_fits<T>(kl, ku))
+    return gbtrs_reg_run<T>(n, kl, ku, nrhs, ab, ldab, ipiv, B, ldb, stream, name);
   const int ch = gbtrs_chunk_for<T>((int)kl, (int)ku, 227 * 1024);
   if (ch == 0) {
     set_error("%s: band too wide for the staged solve", name);
@@ -416,10 +431,12 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
   return launch_status(name);
 }
 
-// Shared memory of one group solving systems up to (kl, ku), 16-byte rounded, in T.
-template <typename T>
-static i64 group_elems(i64 kl, i64 ku, bool /*wide*/) {
-  const i64 e = std::max(gbtrf_smem_elems<kP>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku));
+// Shared memory of one group (NLMAX lanes) solving systems up to (kl, ku), 16-byte
+// rounded, in T.
+template <typename T, int NLMAX>
+static i64 group_elems(i64 kl, i64 ku) {
+  const i64 e = std::max(std::max(gbtrf_smem_elems<kP>((int)kl, (int)ku), gbtrs_smem_elems((int)kl, (int)ku)),
+                         (i64)((reg_group_bytes<T, NLMAX, kMaxRhs>(kl, ku) + (long long)sizeof(T) - 1) / (long long)sizeof(T)));
   return ((e * (i64)sizeof(T) + 15) / 16) * 16 / (i64)sizeof(T);
 }
 
@@ -427,8 +444,8 @@ template <typename T, int W>
 static int gbsv_batched_launch(i64 count, const bm_gb_desc* descs, const int32_t* order, const bm_gb_schedule& sc,
                                T* AB, i64* ipiv, T* B, i64* info, int32_t* counter, cudaStream_t stream,
                                const char* name) {
-  const i64 we = sc.n_wide > 0 ? group_elems<T>(sc.wide_kl, sc.wide_ku, true) : 0;
-  const i64 ne = sc.n_wide < count ? group_elems<T>(sc.narrow_kl, sc.narrow_ku, false) : 0;
+  const i64 we = sc.n_wide > 0 ? group_elems<T, 32 * W>(sc.wide_kl, sc.wide_ku) : 0;
+  const i64 ne = sc.n_wide < count ? group_elems<T, 32>(sc.narrow_kl, sc.narrow_ku) : 0;
   const i64 elems = std::max(std::max(we, W * ne), (i64)kHdr);
   const i64 bytes = elems * (i64)sizeof(T);
   if (bytes > 227 * 1024) {

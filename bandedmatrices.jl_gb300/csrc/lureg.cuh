@@ -77,15 +77,47 @@ struct __align__(16) RegShared {
   long long info;
 };
 
-// Size classes of the register window and the lanes a band needs.
+// Size classes of the register window: 4, 8, 16, 32, then multiples of 16 up to 128.
+// Class K holds the sizes (reg_cls_lo(K), K] ([0, 4] for K = 4).
 constexpr int kRegMaxWarps = 8;
 template <typename T>
 __host__ __device__ constexpr int reg_kl_max() { return sizeof(T) == 4 ? 64 : 32; }
+__host__ __device__ constexpr int reg_cls(long long x) {
+  return x <= 4 ? 4 : x <= 8 ? 8 : x <= 16 ? 16 : x <= 32 ? 32 : (int)((x + 15) / 16 * 16);
+}
+__host__ __device__ constexpr int reg_cls_lo(int K) {
+  return K == 4 ? 0 : K == 8 ? 5 : K == 16 ? 9 : K == 32 ? 17 : K - 15;
+}
 template <typename T>
 __host__ __device__ inline int reg_class(long long kl, long long ku) {
   if (kl < 0 || ku < 0 || kl > reg_kl_max<T>() || kl + ku + 1 > 32 * kRegMaxWarps) return 0;
-  return kl <= 4 ? 4 : kl <= 8 ? 8 : kl <= 16 ? 16 : kl <= 32 ? 32 : 64;
+  return reg_cls(kl);
 }
+template <typename T>
+__host__ __device__ inline int reg_kv_class(long long kv) {
+  if (kv < 0 || kv > 2 * reg_kl_max<T>()) return 0;
+  return reg_cls(kv);
+}
+
+// f(RegK<K>{}) for a class K <= KMAX (callers pass valid classes only).
+template <int K>
+struct RegK {
+  static constexpr int v = K;
+};
+template <int KMAX, typename F>
+__host__ __device__ inline auto reg_dispatch(int K, F&& f) {
+#define BM_RK(k) \
+  case k:        \
+    if constexpr (k <= KMAX) return f(RegK<k>{});
+  switch (K) {
+    BM_RK(8) BM_RK(16) BM_RK(32) BM_RK(48) BM_RK(64) BM_RK(80) BM_RK(96) BM_RK(112) BM_RK(128)
+    default:
+      break;
+  }
+#undef BM_RK
+  return f(RegK<4>{});
+}
+
 __host__ __device__ inline int reg_warps(long long kl, long long ku) { return (int)((kl + ku + 1 + 31) / 32); }
 
 // u = w[d]; w[d] = w[0]  (the interchange of rows j and j+d, 0 < d <= KL), by
@@ -103,26 +135,13 @@ __device__ __forceinline__ T reg_interchange(RegArr<T, KL + 1>& w, int d) {
   return u;
 }
 
-#define BM_RE1(p) \
-  case p:                       \
-    if constexpr ((p) <= KL) {  \
-      w[p] = v;                 \
-    }                           \
-    break;
-#define BM_RE4(p) BM_RE1(p) BM_RE1(p + 1) BM_RE1(p + 2) BM_RE1(p + 3)
-#define BM_RE16(p) BM_RE4(p) BM_RE4(p + 4) BM_RE4(p + 8) BM_RE4(p + 12)
-#define BM_RE64(p) BM_RE16(p) BM_RE16(p + 16) BM_RE16(p + 32) BM_RE16(p + 48)
-
-// w[k] = v  (k <= KL)
+// w[k] = v for a k of the size class KL, by selects over the class's positions (an
+// indexed jump costs several hundred cycles).
 template <typename T, int KL>
 __device__ __forceinline__ void reg_set(RegArr<T, KL + 1>& w, int k, T v) {
-  switch (k) {
-    BM_RE64(0)
-    BM_RE64(64)
-    BM_RE1(128)
-    default:
-      break;
-  }
+  constexpr int lo = reg_cls_lo(KL);
+#pragma unroll
+  for (int p = lo; p <= KL; ++p) w[p] = p == k ? v : w[p];
 }
 
 // The rank-1 update fused with the slide: w[r-1] = fma(l[r-1], nu, w[r]), r = 1..KL.
@@ -138,18 +157,53 @@ __device__ __forceinline__ void reg_update(RegArr<T, KL + 1>& w, const T* __rest
 }
 
 // The same with the plain slide w[r-1] = w[r] where !doit (u == 0 or a zero pivot, as
-// dgbtf2 skips those columns), by selects rather than a divergent branch.
+// dgbtf2 skips those columns), by selects rather than a divergent branch.  The
+// multipliers are read from shared memory kRegLookahead vectors ahead of their use,
+// so their latency overlaps the arithmetic of the preceding rows.
+constexpr int kRegLookahead = 4;
 template <typename T, int KL>
 __device__ __forceinline__ void reg_update_sel(RegArr<T, KL + 1>& w, const T* __restrict__ l, T nu, bool doit) {
   using V = RegVec<T>;
+  using VT = typename V::type;
+  constexpr int NG = KL / V::n, D = kRegLookahead < NG ? kRegLookahead : NG;
+  const VT* lv = reinterpret_cast<const VT*>(l);
+  VT buf[D];
 #pragma unroll
-  for (int q = 0; q < KL; q += V::n) {
-    const typename V::type lv = *reinterpret_cast<const typename V::type*>(l + q);
+  for (int g = 0; g < D; ++g) buf[g] = lv[g];
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    const VT cur = buf[g % D];
+    if (g + D < NG) buf[g % D] = lv[g + D];
 #pragma unroll
     for (int k = 0; k < V::n; ++k) {
-      const T f = fma(V::get(lv, k), nu, w[q + k + 1]);
-      w[q + k] = doit ? f : w[q + k + 1];
+      const int q = g * V::n + k;
+      const T f = fma(V::get(cur, k), nu, w[q + 1]);
+      w[q] = doit ? f : w[q + 1];
     }
+  }
+}
+
+// The same with a branch: for the solves, where b(j) == 0 is rare.
+template <typename T, int KL>
+__device__ __forceinline__ void reg_update_br(RegArr<T, KL + 1>& w, const T* __restrict__ l, T nu, bool doit) {
+  using V = RegVec<T>;
+  using VT = typename V::type;
+  if (doit) {
+    constexpr int NG = KL / V::n, D = kRegLookahead < NG ? kRegLookahead : NG;
+    const VT* lv = reinterpret_cast<const VT*>(l);
+    VT buf[D];
+#pragma unroll
+    for (int g = 0; g < D; ++g) buf[g] = lv[g];
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const VT cur = buf[g % D];
+      if (g + D < NG) buf[g % D] = lv[g + D];
+#pragma unroll
+      for (int k = 0; k < V::n; ++k) w[g * V::n + k] = fma(V::get(cur, k), nu, w[g * V::n + k + 1]);
+    }
+  } else {
+#pragma unroll
+    for (int r = 1; r <= KL; ++r) w[r - 1] = w[r];
   }
 }
 
@@ -281,7 +335,7 @@ __device__ __forceinline__ void reg_pivot(i64 jn, int ol, int lane, i64 m, int k
 // The factorization by one group: tid in [0, NL), NL = 32 * warps >= kl+ku+1; `cta`:
 // the group is the whole CTA (else one warp).  Returns dgbtf2's info.
 template <typename T, int KL, int NLMAX>
-__device__ i64 gbtrf_reg(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab, i64* __restrict__ ipiv,
+__device__ __noinline__ i64 gbtrf_reg(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 ldab, i64* __restrict__ ipiv,
                          RegShared<T, KL, NLMAX>& sh, int tid, int NL, bool cta) {
   constexpr int P = kRegPre;
   const int kv = kl + ku, lane = tid & 31, wig = tid >> 5;
@@ -360,6 +414,205 @@ __device__ i64 gbtrf_reg(i64 m, i64 n, int kl, int ku, T* __restrict__ ab, i64 l
   return sh.info;
 }
 
+// ------------------------------------------------------------ solves, trans = 'N'
+// One warp; lane r sweeps right-hand side r (nr <= R <= 32) keeping its window of b in
+// registers, exactly as the factorization keeps a column: the forward sweep (dgbtrs:
+// interchange, then b(j+1:j+lm) -= b(j) * l, skipped when b(j) == 0) with rows j..j+kl,
+// the back substitution (dtbsv 'U','N': x(j) /= U(j,j), then x(j-p) -= x(j) * U(j-p,j),
+// skipped when x(j) == 0) with rows j..j-kv.  The pivots and L or U columns of a chunk
+// of steps and the rows of b entering the window are copied to shared memory with
+// cp.async one chunk ahead (two buffers).
+template <typename T>
+__host__ __device__ constexpr int reg_chunk() { return sizeof(T) == 4 ? 32 : 16; }
+
+template <typename T, int KL, int R = 32>
+struct __align__(16) RegFwdStage {
+  static constexpr int C = reg_chunk<T>();
+  T l[C][KL];       // multipliers of step j0+i, rows 1..KL
+  T e[C][R];        // row j0+i+1+kl of b, entering the window, per right-hand side
+  long long ip[C];  // ipiv(j0+i)
+};
+template <typename T, int KV, int R = 32>
+struct __align__(16) RegBwdStage {
+  static constexpr int C = reg_chunk<T>();
+  T u[C][KV];  // U(j-p, j), p = 1..KV, of step j = j0-i
+  T e[C][R];   // row j-1-kv of b, entering
+  T dg[C];     // U(j, j)
+};
+
+template <typename T, int KL, int R>
+__device__ __noinline__ void gbtrs_reg_fwd(i64 n, int kl, int ku, int nr, const T* __restrict__ ab, i64 ldab,
+                              const i64* __restrict__ ipiv, T* __restrict__ B, i64 ldb,
+                              RegFwdStage<T, KL, R> (&st)[2], int lane) {
+  constexpr int C = RegFwdStage<T, KL, R>::C;
+  if (kl == 0 || n <= 1) return;
+  const int kv = kl + ku;
+  const bool act = lane < nr;
+  T* b = B + (i64)(act ? lane : 0) * ldb;
+  auto stage = [&](RegFwdStage<T, KL, R>& S, i64 j0) {
+    const int cn = (int)min((i64)C, n - 1 - j0);
+    for (int e = lane; e < cn * KL; e += 32) {
+      const int i = e / KL, q = e - i * KL;
+      const i64 j = j0 + i;
+      const bool ok = q < kl && j + 1 + q < n;
+      cp_async_elem(&S.l[i][q], ok ? ab + (kv + 1 + q) + j * ldab : ab, ok);
+    }
+    for (int i = lane; i < cn; i += 32)
+      cp_async_elem(&S.ip[i], reinterpret_cast<const long long*>(ipiv) + j0 + i, true);
+    for (int e = lane; e < cn * nr; e += 32) {
+      const int r = e / cn, i = e - r * cn;
+      const i64 row = j0 + i + 1 + kl;
+      cp_async_elem(&S.e[i][r], row < n ? B + (i64)r * ldb + row : B, row < n);
+    }
+    cp_async_commit();
+  };
+  __syncwarp();
+  stage(st[0], 0);
+  RegArr<T, KL + 1> w;
+#pragma unroll
+  for (int r = 0; r <= KL; ++r) w[r] = (act && r <= kl && r < n) ? b[r] : T(0);
+  int k = 0;
+  for (i64 j0 = 0; j0 < n - 1; j0 += C, k ^= 1) {
+    const int cn = (int)min((i64)C, n - 1 - j0);
+    cp_async_wait<0>();
+    __syncwarp();
+    if (j0 + C < n - 1) stage(st[k ^ 1], j0 + C);
+    const RegFwdStage<T, KL, R>& S = st[k];
+    for (int i = 0; i < cn; ++i) {
+      const int d = (int)(S.ip[i] - 1 - (j0 + i));
+      T u = w[0];
+      if (d != 0) u = reg_interchange<T, KL>(w, d);
+      if (act) b[j0 + i] = u;
+      reg_update_br<T, KL>(w, S.l[i], -u, is_nonzero(u));
+      reg_set<T, KL>(w, kl, S.e[i][lane < R ? lane : 0]);
+    }
+  }
+  if (act) b[n - 1] = w[0];
+  __syncwarp();
+}
+
+template <typename T, int KV, int R>
+__device__ __noinline__ void gbtrs_reg_bwd(i64 n, int kv, int nr, const T* __restrict__ ab, i64 ldab, T* __restrict__ B, i64 ldb,
+                              RegBwdStage<T, KV, R> (&st)[2], int lane) {
+  constexpr int C = RegBwdStage<T, KV, R>::C;
+  if (n <= 0) return;
+  const bool act = lane < nr;
+  T* b = B + (i64)(act ? lane : 0) * ldb;
+  auto stage = [&](RegBwdStage<T, KV, R>& S, i64 j0) {
+    const int cn = (int)min((i64)C, j0 + 1);
+    for (int e = lane; e < cn * KV; e += 32) {
+      const int i = e / KV, q = e - i * KV;
+      const bool ok = q < kv;
+      cp_async_elem(&S.u[i][q], ok ? ab + (kv - 1 - q) + (j0 - i) * ldab : ab, ok);
+    }
+    for (int i = lane; i < cn; i += 32) cp_async_elem(&S.dg[i], ab + kv + (j0 - i) * ldab, true);
+    for (int e = lane; e < cn * nr; e += 32) {
+      const int r = e / cn, i = e - r * cn;
+      const i64 row = j0 - i - 1 - kv;
+      cp_async_elem(&S.e[i][r], row >= 0 ? B + (i64)r * ldb + row : B, row >= 0);
+    }
+    cp_async_commit();
+  };
+  __syncwarp();
+  stage(st[0], n - 1);
+  RegArr<T, KV + 1> w;  // w[p] = x(j - p)
+#pragma unroll
+  for (int p = 0; p <= KV; ++p) w[p] = (act && p <= kv && n - 1 - p >= 0) ? b[n - 1 - p] : T(0);
+  int k = 0;
+  for (i64 j0 = n - 1; j0 >= 0; j0 -= C, k ^= 1) {
+    const int cn = (int)min((i64)C, j0 + 1);
+    cp_async_wait<0>();
+    __syncwarp();
+    if (j0 - C >= 0) stage(st[k ^ 1], j0 - C);
+    const RegBwdStage<T, KV, R>& S = st[k];
+    for (int i = 0; i < cn; ++i) {
+      const T x0 = w[0];
+      const bool nz = is_nonzero(x0);
+      const T xj = nz ? x0 / S.dg[i] : x0;
+      if (act) b[j0 - i] = xj;
+      reg_update_br<T, KV>(w, S.u[i], -xj, nz);
+      reg_set<T, KV>(w, kv, S.e[i][lane < R ? lane : 0]);
+    }
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------ per-system dispatch
+// For kernels that take systems of different bands: the size class is chosen per
+// system.  A group of NL lanes (NL <= NLMAX) factors with the register window when
+// kl+ku+1 <= NL; the solve runs in the group's first warp.  `smem` must hold
+// reg_smem_bytes<T, NLMAX, R>(kl, ku).
+template <typename T>
+__host__ __device__ inline bool reg_fits(long long kl, long long ku, int NL) {
+  return reg_class<T>(kl, ku) != 0 && kl + ku + 1 <= NL;
+}
+template <typename T>
+__host__ __device__ inline bool reg_solve_fits(long long kl, long long ku) {
+  return reg_class<T>(kl, 0) != 0 && reg_kv_class<T>(kl + ku) != 0;
+}
+template <typename T, int NLMAX, int R>
+__host__ __device__ inline long long reg_smem_bytes(long long kl, long long ku) {
+  constexpr int KM = reg_kl_max<T>();
+  long long f = 0, s = 0, b = 0;
+  if (const int kc = reg_class<T>(kl, ku))
+    f = reg_dispatch<KM>(kc, [&](auto k) { return (long long)sizeof(RegShared<T, decltype(k)::v, NLMAX>); });
+  if (reg_solve_fits<T>(kl, ku)) {
+    s = reg_dispatch<KM>(reg_class<T>(kl, 0), [&](auto k) { return 2 * (long long)sizeof(RegFwdStage<T, decltype(k)::v, R>); });
+    b = reg_dispatch<2 * KM>(reg_kv_class<T>(kl + ku),
+                             [&](auto k) { return 2 * (long long)sizeof(RegBwdStage<T, decltype(k)::v, R>); });
+  }
+  return f > s ? (f > b ? f : b) : (s > b ? s : b);
+}
+
+// Bytes covering every system whose band is within (kl_max, ku_max).
+template <typename T, int NLMAX, int R>
+inline long long reg_group_bytes(long long kl_max, long long ku_max) {
+  long long m = 0;
+  const long long km = kl_max < reg_kl_max<T>() ? kl_max : reg_kl_max<T>();
+  for (long long kl = 0; kl <= km; ++kl) {
+    const long long kum = ku_max < 2 * reg_kl_max<T>() - kl ? ku_max : 2 * reg_kl_max<T>() - kl;
+    for (long long ku = 0; ku <= kum; ku += (ku + 16 <= kum ? 16 : 1)) {
+      const long long b = reg_smem_bytes<T, NLMAX, R>(kl, ku);
+      m = b > m ? b : m;
+    }
+    const long long b = reg_smem_bytes<T, NLMAX, R>(kl, kum);
+    m = b > m ? b : m;
+  }
+  return m;
+}
+
+template <typename T, int NLMAX>
+__device__ i64 gbtrf_reg_any(i64 m, i64 n, int kl, int ku, T* ab, i64 ldab, i64* ipiv, void* smem, int tid, int NL,
+                             bool cta) {
+  return reg_dispatch<reg_kl_max<T>()>(reg_class<T>(kl, ku), [&](auto k) -> i64 {
+    constexpr int K = decltype(k)::v;
+    return gbtrf_reg<T, K, NLMAX>(m, n, kl, ku, ab, ldab, ipiv, *reinterpret_cast<RegShared<T, K, NLMAX>*>(smem), tid,
+                                  NL, cta);
+  });
+}
+
+// gbtrs 'N' for nr right-hand sides (any number; R at a time) by one warp.
+template <typename T, int R>
+__device__ void gbtrs_reg_any(i64 n, int kl, int ku, int nr, const T* ab, i64 ldab, const i64* ipiv, T* B, i64 ldb,
+                              void* smem, int lane) {
+  for (int r0 = 0; r0 < nr; r0 += R) {
+    const int q = min(R, nr - r0);
+    T* Bq = B + (i64)r0 * ldb;
+    reg_dispatch<reg_kl_max<T>()>(reg_class<T>(kl, 0), [&](auto k) {
+      constexpr int K = decltype(k)::v;
+      gbtrs_reg_fwd<T, K, R>(n, kl, ku, q, ab, ldab, ipiv, Bq, ldb, *reinterpret_cast<RegFwdStage<T, K, R>(*)[2]>(smem),
+                             lane);
+      return 0;
+    });
+    reg_dispatch<2 * reg_kl_max<T>()>(reg_kv_class<T>(kl + ku), [&](auto k) {
+      constexpr int K = decltype(k)::v;
+      gbtrs_reg_bwd<T, K, R>(n, kl + ku, q, ab, ldab, Bq, ldb, *reinterpret_cast<RegBwdStage<T, K, R>(*)[2]>(smem),
+                             lane);
+      return 0;
+    });
+  }
+}
+
 }  // namespace bm
 
 namespace bm {
@@ -368,4 +621,9 @@ namespace bm {
 template <typename T>
 int gbtrf_reg_run(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
                   const char* name);
+// gbtrs 'N' by one warp per 32 right-hand sides; callers check reg_class<T>(kl, 0) and
+// reg_kv_class<T>(kl + ku) first.
+template <typename T>
+int gbtrs_reg_run(i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, i64 ldab, const i64* ipiv, T* B, i64 ldb,
+                  cudaStream_t stream, const char* name);
 }  // namespace bm

@@ -14,6 +14,7 @@
 // the O(n kl (kl+ku)) factorization and the triangular solves run in FP32, where
 // GB300 has 64x the FP64 throughput.
 #include "lu.cuh"
+#include "lureg.cuh"
 
 namespace bm {
 
@@ -152,8 +153,19 @@ __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
       }
     }
     sync();
-    // ---- FP32 factorization
-    const i64 inf = gbtrf_group<float, 4, G>(n, n, kl, ku, A32, ldab, ip, smem);
+    // ---- FP32 factorization: the register window where the band fits the group
+    const bool regf = reg_fits<float>(kl, ku, NT);
+    const bool regs = reg_solve_fits<float>(kl, ku);
+    const i64 inf = regf ? gbtrf_reg_any<float, NT>(n, n, kl, ku, A32, ldab, ip, smem, tid, NT, G > 1)
+                         : gbtrf_group<float, 4, G>(n, n, kl, ku, A32, ldab, ip, smem);
+    sync();
+    auto solve32 = [&](int nr, float* R) {
+      if (regs) {
+        if (wig == 0) gbtrs_reg_any<float, kMaxRhs>(n, kl, ku, nr, A32, ldab, ip, R, n, smem, tid & 31);
+      } else {
+        gbtrs_all<float, G>(false, n, kl, ku, nr, A32, ldab, ip, R, n, smem);
+      }
+    };
     if (tid == 0) p.info[s] = inf;
     int its_max = 0;
     double berr_max = 0.0;
@@ -168,7 +180,7 @@ __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
         Rs[e] = (float)Bs[i + c * d.ldb];
       }
       sync();
-      gbtrs_all<float, G>(false, n, kl, ku, nr_all, A32, ldab, ip, Rs, n, smem);
+      solve32(nr_all, Rs);
       sync();
       for (i64 e = tid; e < n * nr_all; e += NT) {
         const i64 c = e / n, i = e - c * n;
@@ -207,7 +219,7 @@ __device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
           }
           if (!(be > p.tol) || it >= p.maxit) break;  // NaN stops too
           sync();
-          gbtrs_all<float, G>(false, n, kl, ku, nr, A32, ldab, ip, Rc, n, smem);
+          solve32(nr, Rc);
           sync();
           for (i64 e = tid; e < n * nr; e += NT) {
             const i64 c = e / n, i = e - c * n;
@@ -259,18 +271,19 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
 // Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window,
 // FP32 solve chunk, FP64 residual scratch; 0 when the refined solve does not support
 // the band (kl + ku above the residual window).
-static i64 mixed_group_elems(i64 kl, i64 ku, bool wide) {
+template <int NLMAX>
+static i64 mixed_group_elems(i64 kl, i64 ku) {
   if (kl + ku + 32 > 32 * kResQWide) return 0;
-  (void)wide;
   const i64 fac = gbtrf_smem_elems<4>((int)kl, (int)ku);
-  const i64 f = std::max(std::max(fac, gbtrs_smem_elems((int)kl, (int)ku)), (i64)(kHdr + 16));
+  const i64 reg = (reg_group_bytes<float, NLMAX, kMaxRhs>(kl, ku) + 3) / 4;
+  const i64 f = std::max(std::max(std::max(fac, gbtrs_smem_elems((int)kl, (int)ku)), (i64)(kHdr + 16)), reg);
   return ((f + 3) / 4) * 4;
 }
 
 template <int W, int Q>
 static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
-  const i64 we = sc.n_wide > 0 ? mixed_group_elems(sc.wide_kl, sc.wide_ku, true) : 1;
-  const i64 ne = sc.n_wide < p.count ? mixed_group_elems(sc.narrow_kl, sc.narrow_ku, false) : 1;
+  const i64 we = sc.n_wide > 0 ? mixed_group_elems<32 * W>(sc.wide_kl, sc.wide_ku) : 1;
+  const i64 ne = sc.n_wide < p.count ? mixed_group_elems<32>(sc.narrow_kl, sc.narrow_ku) : 1;
   if (we == 0 || ne == 0) {
     set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQWide - 32);
     return BM_ERR_UNSUPPORTED;

@@ -35,7 +35,11 @@ def rel(a, b):
 @pytest.mark.parametrize("n,l,u,shift", [(1, 0, 0, 0.0), (2, 1, 1, 0.0), (5, 1, 1, 0.0), (50, 2, 3, 0.0),
                                          (300, 4, 3, 0.0), (300, 4, 3, 10.0), (200, 30, 2, 0.0), (200, 2, 30, 0.0),
                                          (257, 33, 70, 0.0), (400, 64, 64, 0.0), (1000, 7, 0, 0.0),
-                                         (1000, 0, 7, 0.0), (10000, 4, 3, 10.0), (3000, 16, 16, 0.0)])
+                                         (1000, 0, 7, 0.0), (10000, 4, 3, 10.0), (3000, 16, 16, 0.0),
+                                         # every register-window size class of kl and kl + ku
+                                         (300, 40, 8, 0.0), (300, 49, 30, 0.0), (300, 20, 70, 0.0),
+                                         (300, 12, 100, 0.0), (500, 56, 40, 5.0), (260, 6, 2, 0.0),
+                                         (260, 12, 3, 0.0), (260, 24, 8, 0.0)])
 def test_gbtrf_gbtrs_bitexact(bm, gpu, orc, dt, n, l, u, shift):
     rng = np.random.default_rng(n * 131 + l * 7 + u)
     data = rng.standard_normal((l + u + 1, n)).astype(dt)
