@@ -79,7 +79,7 @@ class BandedBatch:
                          self.ip_off], axis=1).astype(np.int64)
         self.descs = torch.from_numpy(np.ascontiguousarray(desc)).to(self.device)
         self.order = torch.from_numpy(lpt_order(self.n, self.kl, self.ku, self.nrhs)).to(self.device)
-        self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)  # work queues (4 for solve_mixed)
         self.max_kl = int(self.kl.max()) if self.count else 0
         self.max_ku = int(self.ku.max()) if self.count else 0
         self.schedule = None  # None: the single-part entry points (bm_*gbsv_batched)

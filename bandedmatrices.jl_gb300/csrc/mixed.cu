@@ -2,110 +2,35 @@
 // spec addition beside lu!/ldiv!, src/banded/BandedLU.jl:90-103,
 // src/banded/linalg.jl:24-30).
 //
-// Per system (one warp): the FP64 band A is rounded to an FP32 copy in gbtrf
-// storage and factored in FP32 with partial pivoting (the same warp algorithm as
-// the FP64 path, lu.cuh).  Then, for each right-hand side b,
-//     x = FP64(LU32 \ FP32(b))
-//     repeat: r = b - A x            (FP64, from the original FP64 band)
-//             berr = ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+// Per system s the FP64 band A is rounded to an FP32 copy in gbtrf storage and
+// factored in FP32 with partial pivoting (the group algorithms of lu.cuh /
+// lureg.cuh).  Then, for its right-hand sides B,
+//     X = FP64(LU32 \ FP32(B))
+//     repeat: R = B - A X                    (FP64, from the original FP64 band)
+//             berr = max_c ||r_c||_inf / (||A||_inf ||x_c||_inf + ||b_c||_inf)
 //             stop when berr <= tol or after maxit corrections
-//             x = x + FP64(LU32 \ FP32(r))
+//             X = X + FP64(LU32 \ FP32(R))
 // The residual and the update, the steps whose stability needs it, run in FP64;
 // the O(n kl (kl+ku)) factorization and the triangular solves run in FP32, where
-// GB300 has 64x the FP64 throughput.
+// GB300 has 74x the FP64 throughput.
+//
+// The solve is a sequence of launches, each shaped for its own bound:
+//   factor   -- one group per system (a warp, or a CTA for wide bands): rounding,
+//               FP32 LU, first solve.  Latency-bound column chains.
+//   residual -- one CTA per system, one lane per row: the FP64 residual of up to
+//               8 right-hand sides per pass over A, diagonal by diagonal, so every
+//               lane of every DFMA does useful work.  Bounded by GB300's FP64 pipe
+//               (1/74 of the FP32 rate), the cost this design minimises.
+//   correct  -- one warp per system: the FP32 correction solve and X += d.
+// `residual` and `correct` alternate maxit times; systems that have converged are
+// skipped, and once every system has converged the launches return at once.
 #include "lu.cuh"
 #include "lureg.cuh"
 
 namespace bm {
 
-// R = B - A X on rows [rb, re) for up to kResRhs right-hand sides of one system,
-// written to R32 (FP32, leading dim n); returns this warp's partial maxima of |r_c|,
-// |x_c| (over the columns it read) and, with want_anorm, of the |A| row sums.  Each
-// lane owns window rows w = lane + 32q (q < kResQ) in registers; band columns are
-// streamed once per 32-column chunk, every lane reading the entry of its own row (a
-// coalesced read of the column), so no shared memory and no synchronisation are
-// needed.  Row i accumulates its terms in ascending column order.
-constexpr int kResRhs = 4;
-constexpr int kResQ = 5;      // window rows 32*Q >= 32 + kl + ku: Q = 5 for kl + ku <= 128,
-constexpr int kResQWide = 9;  // Q = 9 for kl + ku <= 256 (chosen per launch)
-
-template <int kResQ>
-__device__ void residual_rows(i64 n, i64 rb, i64 re, int kl, int ku, int nr, const double* __restrict__ band,
-                              i64 ldab, const double* __restrict__ B, const double* __restrict__ X, i64 ld,
-                              float* __restrict__ R32, bool want_anorm, double& anorm, double* rnorm,
-                              double* xnorm) {
-  const int lane = threadIdx.x & 31;
-  const int kv = kl + ku;  // band: A(i,j) = band[(ku + i - j) + j*ldab]
-  double Y[kResQ][kResRhs], S[kResQ];
-#pragma unroll
-  for (int q = 0; q < kResQ; ++q) {
-    S[q] = 0.0;
-#pragma unroll
-    for (int c = 0; c < kResRhs; ++c) Y[q][c] = 0.0;
-  }
-  double rn[kResRhs], xn[kResRhs], an = 0.0;
-#pragma unroll
-  for (int c = 0; c < kResRhs; ++c) rn[c] = xn[c] = 0.0;
-
-  auto emit = [&](int q, i64 i) {
-    if (i < rb || i >= re) return;
-#pragma unroll
-    for (int c = 0; c < kResRhs; ++c)
-      if (c < nr) {
-        const double ri = B[i + c * ld] - Y[q][c];
-        R32[i + c * n] = (float)ri;
-        rn[c] = fmax(rn[c], fabs(ri));
-      }
-    an = fmax(an, S[q]);
-  };
-
-  const i64 cb = max((i64)0, rb - kl), ce = min(n, re + ku);
-  for (i64 j0 = cb; j0 < ce; j0 += 32) {
-    const int jn = (int)min((i64)32, ce - j0);
-    // window row w <-> matrix row j0 - ku + w;  column j0 + t touches w = t .. t + kv
-    for (int t = 0; t < jn; ++t) {
-      const i64 j = j0 + t;
-      const double* col = band + j * ldab;
-      double xj[kResRhs];
-#pragma unroll
-      for (int c = 0; c < kResRhs; ++c) {
-        xj[c] = c < nr ? X[j + c * ld] : 0.0;
-        xn[c] = fmax(xn[c], fabs(xj[c]));
-      }
-#pragma unroll
-      for (int q = 0; q < kResQ; ++q) {
-        const int r = lane + 32 * q - t;  // band row for this lane's window row
-        const i64 i = j0 - ku + lane + 32 * q;
-        if (r >= 0 && r <= kv && i >= 0 && i < n) {
-          const double a = col[r];
-#pragma unroll
-          for (int c = 0; c < kResRhs; ++c) Y[q][c] = fma(a, xj[c], Y[q][c]);
-          if (want_anorm) S[q] += fabs(a);
-        }
-      }
-    }
-    if (j0 + 32 < ce) {
-      emit(0, j0 - ku + lane);  // rows j0-ku .. j0-ku+31 are complete
-#pragma unroll
-      for (int q = 0; q < kResQ - 1; ++q) {
-        S[q] = S[q + 1];
-#pragma unroll
-        for (int c = 0; c < kResRhs; ++c) Y[q][c] = Y[q + 1][c];
-      }
-      S[kResQ - 1] = 0.0;
-#pragma unroll
-      for (int c = 0; c < kResRhs; ++c) Y[kResQ - 1][c] = 0.0;
-    } else {
-#pragma unroll
-      for (int q = 0; q < kResQ; ++q) emit(q, j0 - ku + lane + 32 * q);
-    }
-  }
-  for (int c = 0; c < kResRhs; ++c) {
-    rnorm[c] = rn[c];
-    xnorm[c] = xn[c];
-  }
-  anorm = an;
-}
+// Corrections per call at most (each is one correction and one residual launch).
+constexpr int kMixedMaxCorrections = 100;
 
 struct MixedParams {
   i64 count;
@@ -117,140 +42,83 @@ struct MixedParams {
   i64* ipiv;
   i64* info;
   float* AB32;       // FP32 factor storage (same offsets as AB)
-  float* R32;        // FP32 work copy of B's layout (leading dim n per system)
-  int32_t* iters;    // per system: corrections taken (max over right-hand sides)
-  double* berr;      // per system: final backward error (max over right-hand sides)
-  int32_t* counter;
+  float* R32;        // FP32 residual / correction (leading dim n per system)
+  int32_t* iters;    // per system: corrections so far (>= 0 while refining, -(k+1) once done)
+  double* berr;      // per system: latest backward error (max over right-hand sides)
+  int32_t* counter;  // 4 int32: work queues and converged-system counts of the two parities
   double tol;
   int maxit;
-  i64 group_elems;   // shared-memory floats per group
+  i64 group_elems;   // shared-memory floats per warp (narrow factor part, correct)
 };
 
-// One system of the batch (index s) by a group of G warps in `smem`; Q sizes the
-// residual's register window.
-template <int G, int Q>
-__device__ void dsgbsv_system(const MixedParams& p, int s, float* smem) {
+// ------------------------------------------------------------------ factor
+template <int G>
+__device__ void mixed_factor_system(const MixedParams& p, int s, float* smem) {
   constexpr int NT = Grp<G>::NT;
   const int tid = Grp<G>::tid(), wig = tid >> 5;
-  double* red = reinterpret_cast<double*>(smem + kHdr);  // reduction scratch (between phases)
   auto sync = [] { Grp<G>::sync(); };
+  const bm_gb_desc d = p.descs[s];
+  const int kl = (int)d.kl, ku = (int)d.ku;
+  const i64 n = d.n, ldab = d.ldab;
+  const double* A = p.AB + d.ab_offset;
+  float* A32 = p.AB32 + d.ab_offset;
+  i64* ip = p.ipiv + d.ipiv_offset;
+  // ---- round to FP32 (the top kl fill-in rows start at zero)
   {
-    const bm_gb_desc d = p.descs[s];
-    const int kl = (int)d.kl, ku = (int)d.ku;
-    const i64 n = d.n, ldab = d.ldab;
-    const double* A = p.AB + d.ab_offset;
-    float* A32 = p.AB32 + d.ab_offset;
-    i64* ip = p.ipiv + d.ipiv_offset;
-    // ---- round to FP32 (the top kl fill-in rows start at zero)
-    {
-      const i64 tot = ldab * n;
-      i64 r = tid;  // row of element e within its column, advanced without division
+    const i64 tot = ldab * n;
+    i64 r = tid;  // row of element e within its column, advanced without division
+    while (r >= ldab) r -= ldab;
+    for (i64 e = tid; e < tot; e += NT) {
+      A32[e] = r < kl ? 0.0f : (float)A[e];
+      r += NT;
       while (r >= ldab) r -= ldab;
-      for (i64 e = tid; e < tot; e += NT) {
-        A32[e] = r < kl ? 0.0f : (float)A[e];
-        r += NT;
-        while (r >= ldab) r -= ldab;
-      }
     }
-    sync();
-    // ---- FP32 factorization: the register window where the band fits the group
-    const bool regf = reg_fits<float>(kl, ku, NT);
-    const bool regs = reg_solve_fits<float>(kl, ku);
-    const i64 inf = regf ? gbtrf_reg_any<float, NT>(n, n, kl, ku, A32, ldab, ip, smem, tid, NT, G > 1)
-                         : gbtrf_group<float, 4, G>(n, n, kl, ku, A32, ldab, ip, smem);
-    sync();
-    auto solve32 = [&](int nr, float* R) {
-      if (regs) {
-        if (wig == 0) gbtrs_reg_any<float, kMaxRhs>(n, kl, ku, nr, A32, ldab, ip, R, n, smem, tid & 31);
-      } else {
-        gbtrs_all<float, G>(false, n, kl, ku, nr, A32, ldab, ip, R, n, smem);
-      }
-    };
-    if (tid == 0) p.info[s] = inf;
-    int its_max = 0;
-    double berr_max = 0.0;
-    if (inf == 0) {
-      const int nr_all = (int)d.nrhs;
-      const double* Bs = p.B + d.b_offset;
-      double* Xs = p.X + d.b_offset;
-      float* Rs = p.R32 + d.b_offset;  // FP32 copy of B's layout (leading dim n)
-      // x0 = LU32 \ b  for every right-hand side
-      for (i64 e = tid; e < n * nr_all; e += NT) {
-        const i64 c = e / n, i = e - c * n;
-        Rs[e] = (float)Bs[i + c * d.ldb];
-      }
-      sync();
-      solve32(nr_all, Rs);
-      sync();
-      for (i64 e = tid; e < n * nr_all; e += NT) {
-        const i64 c = e / n, i = e - c * n;
-        Xs[i + c * d.ldb] = (double)Rs[e];
-      }
-      sync();
-      double anorm = -1.0;  // ||A||_inf, from the first residual pass
-      // this warp's rows in the residual
-      const i64 rb = n * wig / G, re = n * (wig + 1) / G;
-      for (int c0 = 0; c0 < nr_all; c0 += kResRhs) {
-        const int nr = min(kResRhs, nr_all - c0);
-        const double* Bc = Bs + c0 * d.ldb;
-        double* Xc = Xs + c0 * d.ldb;
-        float* Rc = Rs + (i64)c0 * n;
-        double bnorm[kResRhs];
-        for (int c = 0; c < kResRhs; ++c) {
-          double bn = 0.0;
-          if (c < nr)
-            for (i64 i = tid; i < n; i += NT) bn = fmax(bn, fabs(Bc[i + c * d.ldb]));
-          bnorm[c] = grp_max<G>(bn, red);
-        }
-        int it = 0;
-        double be = 0.0;
-        for (;;) {
-          double rnorm[kResRhs], xnorm[kResRhs], an = 0.0;
-          const bool first = anorm < 0.0;
-          residual_rows<Q>(n, rb, re, kl, ku, nr, A + kl, ldab, Bc, Xc, d.ldb, Rc, first, an, rnorm, xnorm);
-          if (first) anorm = grp_max<G>(an, red);
-          be = 0.0;
-          for (int c = 0; c < kResRhs; ++c) {
-            const double rn = grp_max<G>(rnorm[c], red), xn = grp_max<G>(xnorm[c], red);
-            if (c >= nr) continue;
-            const double den = anorm * xn + bnorm[c];
-            const double bc = den > 0.0 ? rn / den : rn;
-            be = (bc > be || bc != bc) ? bc : be;
-          }
-          if (!(be > p.tol) || it >= p.maxit) break;  // NaN stops too
-          sync();
-          solve32(nr, Rc);
-          sync();
-          for (i64 e = tid; e < n * nr; e += NT) {
-            const i64 c = e / n, i = e - c * n;
-            Xc[i + c * d.ldb] += (double)Rc[e];
-          }
-          sync();
-          ++it;
-        }
-        its_max = max(its_max, it);
-        berr_max = (be > berr_max || be != be) ? be : berr_max;
-      }
-    }
-    if (tid == 0) {
-      p.iters[s] = its_max;
-      p.berr[s] = berr_max;
-    }
-    sync();
   }
+  sync();
+  const bool regf = reg_fits<float>(kl, ku, NT);
+  const i64 inf = regf ? gbtrf_reg_any<float, NT>(n, n, kl, ku, A32, ldab, ip, smem, tid, NT, G > 1)
+                       : gbtrf_group<float, 4, G>(n, n, kl, ku, A32, ldab, ip, smem);
+  sync();
+  if (inf == 0) {
+    const int nr = (int)d.nrhs;
+    const double* Bs = p.B + d.b_offset;
+    double* Xs = p.X + d.b_offset;
+    float* Rs = p.R32 + d.b_offset;
+    for (i64 e = tid; e < n * nr; e += NT) {
+      const i64 c = e / n, i = e - c * n;
+      Rs[e] = (float)Bs[i + c * d.ldb];
+    }
+    sync();
+    if (reg_solve_fits<float>(kl, ku)) {
+      if (wig == 0) gbtrs_reg_any<float, kMaxRhs>(n, kl, ku, nr, A32, ldab, ip, Rs, n, smem, tid & 31);
+    } else {
+      gbtrs_all<float, G>(false, n, kl, ku, nr, A32, ldab, ip, Rs, n, smem);
+    }
+    sync();
+    for (i64 e = tid; e < n * nr; e += NT) {
+      const i64 c = e / n, i = e - c * n;
+      Xs[i + c * d.ldb] = (double)Rs[e];
+    }
+  }
+  if (tid == 0) {
+    p.info[s] = inf;
+    p.iters[s] = inf == 0 ? 0 : -1;  // a singular FP32 factor: no refinement
+    p.berr[s] = 0.0;
+  }
+  sync();
 }
 
 // Two-part schedule, as gbsv_batched_kernel: wide systems (order[0..n_wide)) one per
 // CTA of W warps, then narrow systems one per warp in group_elems-float slices.
-template <int W, int Q>
-__global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParams p, i64 n_wide) {
+template <int W>
+__global__ void __launch_bounds__(32 * W) mixed_factor_kernel(const MixedParams p, i64 n_wide) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* base = reinterpret_cast<float*>(smem_raw);
   int idx;
   for (;;) {
     idx = next_item<W>(p.counter, reinterpret_cast<int*>(base));
     if (idx >= n_wide) break;
-    dsgbsv_system<W, Q>(p, p.order ? p.order[idx] : idx, base);
+    mixed_factor_system<W>(p, p.order ? p.order[idx] : idx, base);
     __syncthreads();
   }
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -263,50 +131,343 @@ __global__ void __launch_bounds__(32 * W) dsgbsv_batched_kernel(const MixedParam
       my = __shfl_sync(0xffffffffu, v, 0);
     }
     if (my >= p.count) break;
-    dsgbsv_system<1, Q>(p, p.order ? p.order[my] : my, ws);
+    mixed_factor_system<1>(p, p.order ? p.order[my] : my, ws);
     my = -1;
   }
 }
 
-// Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window,
-// FP32 solve chunk, FP64 residual scratch; 0 when the refined solve does not support
-// the band (kl + ku above the residual window).
+// ------------------------------------------------------------------ residual
+// One CTA of kResW warps per system.  Warp w takes the 32-row tiles w, w+kResW, ...;
+// lane L owns row i = r0 + L and accumulates y_c(i) = sum_j A(i,j) x_c(j) over the
+// diagonals d = j - i = -kl .. ku in ascending order (ascending j, as the row's terms
+// of a gbmv), so every DFMA has all 32 lanes busy.  A tile's diagonals are staged in
+// chunks of 32: A(i, i+d) for the tile's rows (each band column contributes one
+// contiguous run, copied with coalesced cp.async into a skewed [d][row] layout) and
+// the x window the chunk reads, double-buffered per warp.
+constexpr int kResW = 8;    // warps per CTA
+constexpr int kResNR = 8;   // right-hand sides per pass over A
+constexpr int kResDC = 32;  // diagonals per staged chunk
+struct ResWarpStage {
+  double a[kResDC][32];          // a[dd][L] = A(r0+L, r0+L+d0+dd)
+  double x[kResNR][2 * kResDC];  // x[c][k] = x_c(r0+d0+k)
+};
+constexpr int kResSmemBytes = kResW * 2 * (int)sizeof(ResWarpStage) + kResW * (3 * kResNR + 1) * 8 + 64;
+
+// |a| of a double as a float, truncated to 20 mantissa bits, with integer operations
+// only (GB300's FP64 pipe is the residual's bound; the row sums of |A| for ||A||_inf
+// need no more than this accuracy).
+__device__ __forceinline__ float abs_f32_of(double a) {
+  const unsigned hi = (unsigned)__double2hiint(a) & 0x7fffffffu;
+  const int e = (int)(hi >> 20) - 1023 + 127;
+  if (e <= 0) return 0.0f;
+  if (e >= 255) return __int_as_float(0x7f800000);
+  return __uint_as_float(((unsigned)e << 23) | ((hi & 0xfffffu) << 3));
+}
+
+__device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
+__device__ __forceinline__ float nan_maxf(float a, float b) { return (b > a || b != b) ? b : a; }
+
+// The tiles of one warp for right-hand sides [c0, c0+NR): residuals into R32 and the
+// lane's running maxima of |r|, |x|, |b| per right-hand side and of the |A| row sums.
+template <int NR>
+__device__ void residual_tiles(const MixedParams& p, const bm_gb_desc& d, int c0, ResWarpStage* st, int w, int lane,
+                               double* rn, double* xn, double* bn, float& an) {
+  const i64 n = d.n, ldab = d.ldab, ldb = d.ldb;
+  const int kl = (int)d.kl, ku = (int)d.ku;
+  const double* A = p.AB + d.ab_offset;
+  const double* Bs = p.B + d.b_offset + (i64)c0 * ldb;
+  const double* Xs = p.X + d.b_offset + (i64)c0 * ldb;
+  float* Rs = p.R32 + d.b_offset + (i64)c0 * n;
+  const i64 ntiles = (n + 31) >> 5;
+  const int nch = (kl + ku + kResDC) / kResDC;  // chunks of diagonals per tile
+  const i64 my_tiles = ntiles > w ? (ntiles - 1 - w) / kResW + 1 : 0;
+  const i64 items = my_tiles * nch;
+  auto stage = [&](i64 q) {
+    ResWarpStage& S = st[q & 1];
+    const i64 r0 = ((i64)w + (q / nch) * kResW) << 5;
+    const int d0 = -kl + (int)(q % nch) * kResDC;
+    // A: band column j = r0 + d0 + t holds A(i, j) for rows i = r0 + L with
+    // d = j - i in [d0, d0 + 32); the lanes of one t read one contiguous run
+    for (int t = 0; t < 2 * kResDC - 1; ++t) {
+      const int dd = t - lane;
+      if (dd >= 0 && dd < kResDC) {
+        const i64 j = r0 + d0 + t, i = r0 + lane;
+        const int dg = d0 + dd;
+        const bool ok = dg <= ku && i < n && j >= 0 && j < n;
+        cp_async_elem(&S.a[dd][lane], ok ? A + (kl + ku - dg) + j * ldab : A, ok);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const i64 xi = r0 + d0 + lane + 32 * h;
+        const bool ok = xi >= 0 && xi < n;
+        cp_async_elem(&S.x[c][lane + 32 * h], ok ? Xs + xi + c * ldb : Xs, ok);
+      }
+    cp_async_commit();
+  };
+  double y[NR];
+#pragma unroll
+  for (int c = 0; c < NR; ++c) y[c] = 0.0;
+  float sabs = 0.0f;
+  if (items > 0) stage(0);
+  for (i64 q = 0; q < items; ++q) {
+    if (q + 1 < items) {
+      stage(q + 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncwarp();
+    const ResWarpStage& S = st[q & 1];
+    const int ch = (int)(q % nch);
+    const int d0 = -kl + ch * kResDC;
+    const int ndd = min(kResDC, ku - d0 + 1);
+#pragma unroll 4
+    for (int dd = 0; dd < ndd; ++dd) {
+      const double a = S.a[dd][lane];
+      sabs += abs_f32_of(a);
+#pragma unroll
+      for (int c = 0; c < NR; ++c) y[c] = fma(a, S.x[c][lane + dd], y[c]);
+    }
+    __syncwarp();  // the buffer is restaged two items later
+    if (ch == nch - 1) {  // the tile is complete
+      const i64 i = (((i64)w + (q / nch) * kResW) << 5) + lane;
+      if (i < n) {
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          const double b = Bs[i + c * ldb], x = Xs[i + c * ldb];
+          const double r = b - y[c];
+          Rs[i + (i64)c * n] = (float)r;
+          rn[c] = nan_max(rn[c], fabs(r));
+          xn[c] = nan_max(xn[c], fabs(x));
+          bn[c] = nan_max(bn[c], fabs(b));
+        }
+        an = nan_maxf(an, sabs);
+      }
+#pragma unroll
+      for (int c = 0; c < NR; ++c) y[c] = 0.0;
+      sabs = 0.0f;
+    }
+  }
+}
+
+template <int NR>
+__device__ double residual_group(const MixedParams& p, const bm_gb_desc& d, int c0, ResWarpStage* st, double* red) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double rn[NR], xn[NR], bn[NR];
+#pragma unroll
+  for (int c = 0; c < NR; ++c) rn[c] = xn[c] = bn[c] = 0.0;
+  float an = 0.0f;
+  residual_tiles<NR>(p, d, c0, st, w, lane, rn, xn, bn, an);
+  // warp, then CTA maxima (NaN propagates)
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+      rn[c] = nan_max(rn[c], __shfl_xor_sync(0xffffffffu, rn[c], off));
+      xn[c] = nan_max(xn[c], __shfl_xor_sync(0xffffffffu, xn[c], off));
+      bn[c] = nan_max(bn[c], __shfl_xor_sync(0xffffffffu, bn[c], off));
+    }
+    an = nan_maxf(an, __shfl_xor_sync(0xffffffffu, an, off));
+  }
+  double* rw = red + w * (3 * kResNR + 1);
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < NR; ++c) {
+      rw[c] = rn[c];
+      rw[kResNR + c] = xn[c];
+      rw[2 * kResNR + c] = bn[c];
+    }
+    rw[3 * kResNR] = (double)an;
+  }
+  __syncthreads();
+  double be = 0.0;
+  if (threadIdx.x == 0) {
+    double anorm = red[3 * kResNR];
+    for (int k = 1; k < kResW; ++k) anorm = nan_max(anorm, red[k * (3 * kResNR + 1) + 3 * kResNR]);
+    for (int c = 0; c < NR; ++c) {
+      double r = red[c], x = red[kResNR + c], b = red[2 * kResNR + c];
+      for (int k = 1; k < kResW; ++k) {
+        const double* rk = red + k * (3 * kResNR + 1);
+        r = nan_max(r, rk[c]);
+        x = nan_max(x, rk[kResNR + c]);
+        b = nan_max(b, rk[2 * kResNR + c]);
+      }
+      const double den = anorm * x + b;
+      const double bc = den > 0.0 ? r / den : r;
+      be = nan_max(be, bc);
+    }
+  }
+  __syncthreads();
+  return be;  // meaningful in thread 0
+}
+
+// Pass k of the refinement (parity par = k & 1): queue counter[2 par], systems still
+// refining after the pass counted in counter[2 par + 1], systems refining after the
+// previous pass read from counter[2 (1 - par) + 1] (zero: nothing to do).
+__global__ void __launch_bounds__(32 * kResW, 1) mixed_residual_kernel(const MixedParams p, int par) {
+  if (*reinterpret_cast<volatile const int32_t*>(p.counter + 2 * (1 - par) + 1) == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ResWarpStage* st = reinterpret_cast<ResWarpStage*>(smem_raw) + 2 * (threadIdx.x >> 5);
+  double* red = reinterpret_cast<double*>(smem_raw + kResW * 2 * sizeof(ResWarpStage));
+  int* hdr = reinterpret_cast<int*>(red + kResW * (3 * kResNR + 1));
+  int32_t* queue = p.counter + 2 * par;
+  for (;;) {
+    if (threadIdx.x == 0) hdr[0] = atomicAdd(queue, 1);
+    __syncthreads();
+    const int idx = hdr[0];
+    __syncthreads();
+    if (idx >= p.count) break;
+    const int s = p.order ? p.order[idx] : idx;
+    const int it = p.iters[s];
+    if (it < 0) continue;  // converged, or no FP32 factor
+    const bm_gb_desc d = p.descs[s];
+    double be = 0.0;
+    for (int c0 = 0; c0 < (int)d.nrhs; c0 += kResNR) {
+      const int nr = (int)min((i64)kResNR, d.nrhs - c0);
+      double b;
+      switch (nr) {
+        case 1: b = residual_group<1>(p, d, c0, st, red); break;
+        case 2: b = residual_group<2>(p, d, c0, st, red); break;
+        case 3: b = residual_group<3>(p, d, c0, st, red); break;
+        case 4: b = residual_group<4>(p, d, c0, st, red); break;
+        case 5: b = residual_group<5>(p, d, c0, st, red); break;
+        case 6: b = residual_group<6>(p, d, c0, st, red); break;
+        case 7: b = residual_group<7>(p, d, c0, st, red); break;
+        default: b = residual_group<8>(p, d, c0, st, red); break;
+      }
+      be = nan_max(be, b);
+    }
+    if (threadIdx.x == 0) {
+      p.berr[s] = be;
+      if (!(be > p.tol) || it >= p.maxit) p.iters[s] = -(it + 1);  // NaN stops too
+      else atomicAdd(queue + 1, 1);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ correct
+// Correction k (parity par = k & 1): one warp per system still refining solves
+// LU32 d = r in place in R32 and adds d to X in FP64.
+template <int W>
+__global__ void __launch_bounds__(32 * W) mixed_correct_kernel(const MixedParams p, int par) {
+  if (*reinterpret_cast<volatile const int32_t*>(p.counter + 2 * (1 - par) + 1) == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* ws = reinterpret_cast<float*>(smem_raw) + w * p.group_elems;
+  int32_t* queue = p.counter + 2 * par;
+  for (;;) {
+    int v = 0;
+    if (lane == 0) v = atomicAdd(queue, 1);
+    v = __shfl_sync(0xffffffffu, v, 0);
+    if (v >= p.count) break;
+    const int s = p.order ? p.order[v] : v;
+    if (p.iters[s] < 0) continue;
+    const bm_gb_desc d = p.descs[s];
+    const int kl = (int)d.kl, ku = (int)d.ku, nr = (int)d.nrhs;
+    const i64 n = d.n;
+    const float* A32 = p.AB32 + d.ab_offset;
+    const i64* ip = p.ipiv + d.ipiv_offset;
+    float* Rs = p.R32 + d.b_offset;
+    double* Xs = p.X + d.b_offset;
+    if (reg_solve_fits<float>(kl, ku)) gbtrs_reg_any<float, kMaxRhs>(n, kl, ku, nr, A32, d.ldab, ip, Rs, n, ws, lane);
+    else gbtrs_all<float, 1>(false, n, kl, ku, nr, A32, d.ldab, ip, Rs, n, ws);
+    __syncwarp();
+    for (i64 e = lane; e < n * nr; e += 32) {
+      const i64 c = e / n, i = e - c * n;
+      Xs[i + c * d.ldb] += (double)Rs[e];
+    }
+    if (lane == 0) p.iters[s] += 1;
+    __syncwarp();
+  }
+}
+
+// iters: -(k+1) (done after k corrections) -> k
+__global__ void mixed_finish_kernel(i64 count, int32_t* iters) {
+  for (i64 s = blockIdx.x * (i64)blockDim.x + threadIdx.x; s < count; s += (i64)gridDim.x * blockDim.x) {
+    const int v = iters[s];
+    iters[s] = v < 0 ? -v - 1 : v;
+  }
+}
+
+// Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window
+// and solve staging; 0 when the refined solve does not support the band.
 template <int NLMAX>
 static i64 mixed_group_elems(i64 kl, i64 ku) {
-  if (kl + ku + 32 > 32 * kResQWide) return 0;
+  if (kl + ku > 256) return 0;
   const i64 fac = gbtrf_smem_elems<4>((int)kl, (int)ku);
   const i64 reg = (reg_group_bytes<float, NLMAX, kMaxRhs>(kl, ku) + 3) / 4;
   const i64 f = std::max(std::max(std::max(fac, gbtrs_smem_elems((int)kl, (int)ku)), (i64)(kHdr + 16)), reg);
   return ((f + 3) / 4) * 4;
 }
 
-template <int W, int Q>
-static int dsgbsv_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
+template <int W>
+static int mixed_launch(MixedParams p, const bm_gb_schedule& sc, cudaStream_t stream, const char* name) {
   const i64 we = sc.n_wide > 0 ? mixed_group_elems<32 * W>(sc.wide_kl, sc.wide_ku) : 1;
   const i64 ne = sc.n_wide < p.count ? mixed_group_elems<32>(sc.narrow_kl, sc.narrow_ku) : 1;
   if (we == 0 || ne == 0) {
-    set_error("%s: kl + ku exceeds the refined solve's limit of %d", name, 32 * kResQWide - 32);
+    set_error("%s: kl + ku exceeds the refined solve's limit of 256", name);
     return BM_ERR_UNSUPPORTED;
   }
+  // ---- factor
   p.group_elems = sc.n_wide < p.count ? ne : 0;
   const i64 bytes = std::max(std::max(we, W * (sc.n_wide < p.count ? ne : 0)), (i64)kHdr) * 4;
   if (bytes > 227 * 1024) {
     set_error("%s: the schedule's shared memory (%lld bytes) exceeds the per-CTA limit", name, (long long)bytes);
     return BM_ERR_UNSUPPORTED;
   }
-  const void* kfn = (const void*)dsgbsv_batched_kernel<W, Q>;
+  const void* kfn = (const void*)mixed_factor_kernel<W>;
   int r = cuda_status(ensure_smem(kfn, (int)bytes), name);
   if (r) return r;
   int per_sm = 0;
-  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dsgbsv_batched_kernel<W, Q>, 32 * W, (int)bytes),
+  r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_factor_kernel<W>, 32 * W, (int)bytes),
                   name);
   if (r) return r;
   per_sm = std::max(per_sm, 1);
   const i64 need = sc.n_wide + ceil_div(p.count - sc.n_wide, (i64)W);
   const i64 grid = std::min<i64>((i64)num_sms() * per_sm, std::max<i64>(need, 1));
-  r = cuda_status(cudaMemsetAsync(p.counter, 0, sizeof(int32_t), stream), name);
-  if (r) return r;
-  dsgbsv_batched_kernel<W, Q><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(p, sc.n_wide);
+  // counter[3] != 0: the first residual pass has work
+  if ((r = cuda_status(cudaMemsetAsync(p.counter, 0, 4 * sizeof(int32_t), stream), name))) return r;
+  if ((r = cuda_status(cudaMemsetAsync(reinterpret_cast<char*>(p.counter + 3), 1, 1, stream), name))) return r;
+  mixed_factor_kernel<W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(p, sc.n_wide);
+  if ((r = launch_status(name))) return r;
+
+  // ---- correction solves: one warp per system, W warps per CTA
+  const i64 kl_all = std::max(sc.n_wide > 0 ? sc.wide_kl : 0, sc.n_wide < p.count ? sc.narrow_kl : 0);
+  const i64 ku_all = std::max(sc.n_wide > 0 ? sc.wide_ku : 0, sc.n_wide < p.count ? sc.narrow_ku : 0);
+  const i64 ce = std::max(mixed_group_elems<32>(kl_all, ku_all), (i64)kHdr);
+  const int cbytes = (int)(W * ce * 4);
+  if (cbytes > 227 * 1024) {
+    set_error("%s: the correction's shared memory (%d bytes) exceeds the per-CTA limit", name, cbytes);
+    return BM_ERR_UNSUPPORTED;
+  }
+  if ((r = cuda_status(ensure_smem((const void*)mixed_correct_kernel<W>, cbytes), name))) return r;
+  int cper = 0;
+  if ((r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cper, mixed_correct_kernel<W>, 32 * W, cbytes),
+                       name)))
+    return r;
+  const i64 cgrid = std::min<i64>((i64)num_sms() * std::max(cper, 1), std::max<i64>(ceil_div(p.count, (i64)W), 1));
+  // ---- residual passes: one CTA per system
+  if ((r = cuda_status(ensure_smem((const void*)mixed_residual_kernel, kResSmemBytes), name))) return r;
+  const i64 rgrid = std::min<i64>((i64)num_sms(), std::max<i64>(p.count, 1));
+
+  for (int k = 0; k <= p.maxit; ++k) {
+    const int par = k & 1;
+    if (k > 0) {
+      MixedParams q = p;
+      q.group_elems = ce;
+      if ((r = cuda_status(cudaMemsetAsync(p.counter + 2 * par, 0, sizeof(int32_t), stream), name))) return r;
+      mixed_correct_kernel<W><<<(unsigned)cgrid, 32 * W, cbytes, stream>>>(q, par);
+      if ((r = launch_status(name))) return r;
+    }
+    if ((r = cuda_status(cudaMemsetAsync(p.counter + 2 * par, 0, 2 * sizeof(int32_t), stream), name))) return r;
+    mixed_residual_kernel<<<(unsigned)rgrid, 32 * kResW, kResSmemBytes, stream>>>(p, par);
+    if ((r = launch_status(name))) return r;
+  }
+  mixed_finish_kernel<<<(unsigned)std::min<i64>(ceil_div(std::max<i64>(p.count, 1), 256), 1024), 256, 0, stream>>>(
+      p.count, p.iters);
   return launch_status(name);
 }
 
@@ -320,12 +481,8 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
   if (!(p.tol >= 0.0)) return -15;
   if (p.maxit < 0) return -16;
   if (p.count == 0) return BM_OK;
-  const i64 kvmax = std::max(sc->n_wide > 0 ? sc->wide_kl + sc->wide_ku : 0,
-                             sc->n_wide < p.count ? sc->narrow_kl + sc->narrow_ku : 0);
-  const bool wideq = kvmax + 32 > 32 * kResQ;
-  if (sc->warps == 8) return wideq ? dsgbsv_launch<8, kResQWide>(p, *sc, stream, name)
-                                   : dsgbsv_launch<8, kResQ>(p, *sc, stream, name);
-  return wideq ? dsgbsv_launch<4, kResQWide>(p, *sc, stream, name) : dsgbsv_launch<4, kResQ>(p, *sc, stream, name);
+  if (sc->warps == 8) return mixed_launch<8>(p, *sc, stream, name);
+  return mixed_launch<4>(p, *sc, stream, name);
 }
 
 }  // namespace bm
@@ -337,7 +494,7 @@ extern "C" int bm_dsgbsv_batched(int64_t count, const bm_gb_desc* descs, const i
   bm::MixedParams p;
   p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
   p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
-  p.maxit = (int)std::min<int64_t>(maxit, 1 << 20);
+  p.maxit = (int)std::min<int64_t>(maxit, bm::kMixedMaxCorrections);
   p.group_elems = 0;
   if (maxit < 0) return -15;
   if (max_kl < 0) return -17;
@@ -358,7 +515,7 @@ extern "C" int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, c
   bm::MixedParams p;
   p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
   p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
-  p.maxit = (int)std::min<int64_t>(maxit, 1 << 20);
+  p.maxit = (int)std::min<int64_t>(maxit, bm::kMixedMaxCorrections);
   p.group_elems = 0;
   if (maxit < 0) return -16;
   return bm::dsgbsv_batched_impl(p, sched, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched_sched");

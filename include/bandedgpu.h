@@ -214,8 +214,10 @@ int bm_sgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t
  * receives the solutions (B's layout), iters/berr the corrections taken and the
  * final backward error per system (max over its right-hand sides), info the FP32
  * factorization's info.  R32 is FP32 workspace laid out like B but with leading
- * dimension n (n*nrhs floats per system at its b_offset); counter is one int32 of
- * workspace.  kl + ku <= 256 per system.  No counterpart in the
+ * dimension n (n*nrhs floats per system at its b_offset); counter is 4 int32 of
+ * workspace.  kl + ku <= 256 per system; maxit is capped at 100.  The call enqueues
+ * a factor launch, then maxit pairs of correction / FP64-residual launches (pairs
+ * after every system has converged return at once).  No counterpart in the
  * reference; per system it replaces lu! + ldiv! (src/banded/BandedLU.jl:90-103,
  * src/banded/linalg.jl:24-30) when the caller accepts a backward-error target. */
 int bm_dsgbsv_batched(int64_t count, const bm_gb_desc *descs, const int32_t *order, const double *AB,
