@@ -26,6 +26,7 @@
 // skipped, and once every system has converged the launches return at once.
 #include "lu.cuh"
 #include "lureg.cuh"
+#include "mixedlu.cuh"
 
 namespace bm {
 
@@ -392,6 +393,120 @@ __global__ void mixed_finish_kernel(i64 count, int32_t* iters) {
   }
 }
 
+// ------------------------------------------------------------------ blocked path
+// Bands with kl <= 80 and kl + ku <= 151 (and a window that fits shared memory): the
+// blocked FP32 LU by one CTA per system and the warp solves of mixedlu.cuh.
+__global__ void __launch_bounds__(kBlkThreads, 3) mixed_lu_blocked_kernel(const MixedParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* q = reinterpret_cast<int*>(smem_raw + 80);  // the next system (header bytes 80..83)
+  for (;;) {
+    if (threadIdx.x == 0) *q = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int idx = *q;
+    __syncthreads();
+    if (idx >= p.count) break;
+    const int s = p.order ? p.order[idx] : idx;
+    const bm_gb_desc d = p.descs[s];
+    const i64 inf = blk_lu_cta(d.n, (int)d.kl, (int)d.ku, p.AB + d.ab_offset, d.ldab, p.AB32 + d.ab_offset, d.ldab,
+                               p.ipiv + d.ipiv_offset, smem_raw);
+    if (threadIdx.x == 0) {
+      p.info[s] = inf;
+      p.iters[s] = inf == 0 ? 0 : -1;  // a singular FP32 factor: no refinement
+      p.berr[s] = 0.0;
+    }
+  }
+}
+
+// Work item q of a solve launch: system order[q mod count], right-hand sides
+// [0, 4) for q < count and [4, nrhs) for the rest (4 at a time), one warp each.
+// first != 0: the first solve, X = FP64(LU32 \ FP32(B)); else correction k (parity
+// par): LU32 d = r in place in R32 and X += d, for the systems still refining.
+template <int W>
+__global__ void __launch_bounds__(32 * W, 16 / W) mixed_solve_blocked_kernel(const MixedParams p, int par, int first) {
+  if (!first && *reinterpret_cast<volatile const int32_t*>(p.counter + 2 * (1 - par) + 1) == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  float* ring = reinterpret_cast<float*>(smem_raw) + (threadIdx.x >> 5) * kSolveRingFloats;
+  int32_t* queue = p.counter + 2 * par;
+  for (;;) {
+    int v = 0;
+    if (lane == 0) v = atomicAdd(queue, 1);
+    v = __shfl_sync(0xffffffffu, v, 0);
+    if (v >= 2 * p.count) break;
+    const bool tail = v >= p.count;
+    const int s = p.order ? p.order[tail ? v - p.count : v] : (tail ? v - (int)p.count : v);
+    if (p.iters[s] < 0) continue;
+    const bm_gb_desc d = p.descs[s];
+    const i64 n = d.n, nrhs = d.nrhs;
+    if (tail && nrhs <= kSolveNR) continue;
+    if (!first && !tail && lane == 0) p.iters[s] += 1;
+    for (i64 c0 = tail ? kSolveNR : 0; c0 < (tail ? nrhs : min((i64)kSolveNR, nrhs)); c0 += kSolveNR) {
+      const int nr = (int)min((i64)kSolveNR, nrhs - c0);
+      float* Rs = p.R32 + d.b_offset + c0 * n;
+      double* Xs = p.X + d.b_offset + c0 * d.ldb;
+      if (first) {
+        const double* Bs = p.B + d.b_offset + c0 * d.ldb;
+        for (int c = 0; c < nr; ++c)
+          for (i64 i = lane; i < n; i += 32) Rs[i + c * n] = (float)Bs[i + c * d.ldb];
+        __syncwarp();
+      }
+      blk_solve_warp(n, (int)d.kl, (int)d.ku, nr, p.AB32 + d.ab_offset, d.ldab, p.ipiv + d.ipiv_offset, Rs, n, ring,
+                     lane);
+      __syncwarp();
+      for (int c = 0; c < nr; ++c)
+        for (i64 i = lane; i < n; i += 32) {
+          const double r = (double)Rs[i + c * n];
+          if (first) Xs[i + c * d.ldb] = r;
+          else Xs[i + c * d.ldb] += r;
+        }
+      __syncwarp();
+    }
+  }
+}
+
+static int mixed_launch_blocked(MixedParams p, i64 kl_max, i64 ku_max, cudaStream_t stream, const char* name) {
+  constexpr int SW = 4;  // warps per CTA of the solve kernel
+  const int lbytes = (int)blk_smem_bytes(kl_max, ku_max);
+  int r = cuda_status(ensure_smem((const void*)mixed_lu_blocked_kernel, lbytes), name);
+  if (r) return r;
+  int lper = 0;
+  if ((r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper, mixed_lu_blocked_kernel, kBlkThreads,
+                                                                      lbytes),
+                       name)))
+    return r;
+  const i64 lgrid = std::min<i64>((i64)num_sms() * std::max(lper, 1), p.count);
+  const int sbytes = SW * kSolveRingFloats * (int)sizeof(float);
+  if ((r = cuda_status(ensure_smem((const void*)mixed_solve_blocked_kernel<SW>, sbytes), name))) return r;
+  int sper = 0;
+  if ((r = cuda_status(
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sper, mixed_solve_blocked_kernel<SW>, 32 * SW, sbytes), name)))
+    return r;
+  const i64 sgrid = std::min<i64>((i64)num_sms() * std::max(sper, 1), ceil_div(2 * p.count, (i64)SW));
+  if ((r = cuda_status(ensure_smem((const void*)mixed_residual_kernel, kResSmemBytes), name))) return r;
+  const i64 rgrid = std::min<i64>((i64)num_sms(), p.count);
+
+  // counter[3] != 0: the first residual pass has work
+  if ((r = cuda_status(cudaMemsetAsync(p.counter, 0, 4 * sizeof(int32_t), stream), name))) return r;
+  if ((r = cuda_status(cudaMemsetAsync(reinterpret_cast<char*>(p.counter + 3), 1, 1, stream), name))) return r;
+  mixed_lu_blocked_kernel<<<(unsigned)lgrid, kBlkThreads, lbytes, stream>>>(p);
+  if ((r = launch_status(name))) return r;
+  mixed_solve_blocked_kernel<SW><<<(unsigned)sgrid, 32 * SW, sbytes, stream>>>(p, 1, 1);  // queue counter[2]
+  if ((r = launch_status(name))) return r;
+  for (int k = 0; k <= p.maxit; ++k) {
+    const int par = k & 1;
+    if (k > 0) {
+      if ((r = cuda_status(cudaMemsetAsync(p.counter + 2 * par, 0, sizeof(int32_t), stream), name))) return r;
+      mixed_solve_blocked_kernel<SW><<<(unsigned)sgrid, 32 * SW, sbytes, stream>>>(p, par, 0);
+      if ((r = launch_status(name))) return r;
+    }
+    if ((r = cuda_status(cudaMemsetAsync(p.counter + 2 * par, 0, 2 * sizeof(int32_t), stream), name))) return r;
+    mixed_residual_kernel<<<(unsigned)rgrid, 32 * kResW, kResSmemBytes, stream>>>(p, par);
+    if ((r = launch_status(name))) return r;
+  }
+  mixed_finish_kernel<<<(unsigned)std::min<i64>(ceil_div(p.count, 256), 1024), 256, 0, stream>>>(p.count, p.iters);
+  return launch_status(name);
+}
+
 // Floats of one group's shared memory for systems up to (kl, ku): FP32 factor window
 // and solve staging; 0 when the refined solve does not support the band.
 template <int NLMAX>
@@ -481,6 +596,10 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
   if (!(p.tol >= 0.0)) return -15;
   if (p.maxit < 0) return -16;
   if (p.count == 0) return BM_OK;
+  const i64 kl_all = std::max(sc->n_wide > 0 ? sc->wide_kl : 0, sc->n_wide < p.count ? sc->narrow_kl : 0);
+  const i64 ku_all = std::max(sc->n_wide > 0 ? sc->wide_ku : 0, sc->n_wide < p.count ? sc->narrow_ku : 0);
+  if (blk_lu_fits(kl_all, ku_all) && blk_solve_fits(kl_all, ku_all) && blk_smem_bytes(kl_all, ku_all) <= 227 * 1024)
+    return mixed_launch_blocked(p, kl_all, ku_all, stream, name);
   if (sc->warps == 8) return mixed_launch<8>(p, *sc, stream, name);
   return mixed_launch<4>(p, *sc, stream, name);
 }

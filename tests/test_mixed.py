@@ -120,3 +120,40 @@ def test_single_system_refined_wide_and_conditioned(bm, gpu, orc):
     bm.mul_(r, A, x, -1.0, 1.0)
     anorm = float(A.data.abs().sum(0).max())
     assert float(r.abs().max()) / (anorm * float(x.abs().max()) + float(b.abs().max())) <= 1.5e-10
+
+
+def test_mixed_small_zero_bandwidth_and_singular(bm, gpu, orc):
+    """Systems shorter than one 16-column panel, zero bandwidths, bands at the blocked
+    path's limits, and one singular system (a zero column): info reports the zero pivot
+    and that system is not refined; every other system converges to the oracle's
+    solution."""
+    rng = np.random.default_rng(14)
+    shapes = [(1, 0, 0), (2, 1, 0), (2, 0, 1), (5, 3, 3), (15, 2, 7), (16, 16, 0), (17, 0, 16), (33, 5, 1),
+              (40, 12, 30), (100, 0, 0), (300, 63, 64), (257, 64, 31), (50, 4, 4)]
+    n = np.array([s[0] for s in shapes])
+    kl = np.array([s[1] for s in shapes])
+    ku = np.array([s[2] for s in shapes])
+    nrhs = rng.integers(1, 7, len(shapes))
+    sing = len(shapes) - 1
+
+    def shift(s, d):
+        if s == sing:
+            d[:, 3] = 0.0  # column 3 of A is zero: the factorization meets a zero pivot
+            return 0.0
+        return 2.0 * (kl[s] + ku[s]) + 1.0
+
+    batch, data, rhs = _fill(bm, gpu, rng, n, kl, ku, nrhs, shift)
+    batch.solve_mixed(tol=1e-10, maxit=30)
+    torch.cuda.synchronize()
+    info = batch.info.cpu().numpy()
+    assert info[sing] == 4, info
+    ok = np.arange(len(shapes)) != sing
+    assert np.abs(info[ok]).max() == 0
+    berr = batch.berr.cpu().numpy()
+    assert berr[ok].max() <= 1e-10, berr
+    assert batch.iters.cpu().numpy()[sing] == 0
+    for s in np.nonzero(ok)[0]:
+        x = batch.solution(s).cpu().numpy()
+        LU, ipiv, _ = orc.gbtf2(n[s], n[s], kl[s], ku[s], orc.lu_storage(data[s], n[s], kl[s], ku[s]))
+        xr = orc.gbtrs("N", n[s], kl[s], ku[s], LU, ipiv, rhs[s])
+        assert np.abs(x - xr).max() <= 1e-10 * max(1.0, np.abs(xr).max()), s
