@@ -396,7 +396,7 @@ __global__ void mixed_finish_kernel(i64 count, int32_t* iters) {
 // ------------------------------------------------------------------ blocked path
 // Bands with kl <= 80 and kl + ku <= 151 (and a window that fits shared memory): the
 // blocked FP32 LU by one CTA per system and the warp solves of mixedlu.cuh.
-__global__ void __launch_bounds__(kBlkThreads, 3) mixed_lu_blocked_kernel(const MixedParams p) {
+__global__ void __launch_bounds__(kBlkThreads, 4) mixed_lu_blocked_kernel(const MixedParams p, int stage) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* q = reinterpret_cast<int*>(smem_raw + 80);  // the next system (header bytes 80..83)
   for (;;) {
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kBlkThreads, 3) mixed_lu_blocked_kernel(const 
     const int s = p.order ? p.order[idx] : idx;
     const bm_gb_desc d = p.descs[s];
     const i64 inf = blk_lu_cta(d.n, (int)d.kl, (int)d.ku, p.AB + d.ab_offset, d.ldab, p.AB32 + d.ab_offset, d.ldab,
-                               p.ipiv + d.ipiv_offset, smem_raw);
+                               p.ipiv + d.ipiv_offset, smem_raw, stage != 0);
     if (threadIdx.x == 0) {
       p.info[s] = inf;
       p.iters[s] = inf == 0 ? 0 : -1;  // a singular FP32 factor: no refinement
@@ -466,14 +466,22 @@ __global__ void __launch_bounds__(32 * W, 16 / W) mixed_solve_blocked_kernel(con
 
 static int mixed_launch_blocked(MixedParams p, i64 kl_max, i64 ku_max, cudaStream_t stream, const char* name) {
   constexpr int SW = 4;  // warps per CTA of the solve kernel
-  const int lbytes = (int)blk_smem_bytes(kl_max, ku_max);
-  int r = cuda_status(ensure_smem((const void*)mixed_lu_blocked_kernel, lbytes), name);
-  if (r) return r;
-  int lper = 0;
-  if ((r = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper, mixed_lu_blocked_kernel, kBlkThreads,
-                                                                      lbytes),
-                       name)))
+  // the cp.async staging of window slides, unless it costs an SM a CTA
+  int lper = 0, lper_ns = 0, r;
+  const int bytes_s = (int)blk_smem_bytes(kl_max, ku_max, true), bytes_ns = (int)blk_smem_bytes(kl_max, ku_max, false);
+  if ((r = cuda_status(ensure_smem((const void*)mixed_lu_blocked_kernel, std::min(bytes_s, 227 * 1024)), name)))
     return r;
+  if (bytes_s <= 227 * 1024 &&
+      (r = cuda_status(
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper, mixed_lu_blocked_kernel, kBlkThreads, bytes_s), name)))
+    return r;
+  if ((r = cuda_status(
+           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper_ns, mixed_lu_blocked_kernel, kBlkThreads, bytes_ns),
+           name)))
+    return r;
+  const bool stage = lper > 0 && lper >= lper_ns;
+  const int lbytes = stage ? bytes_s : bytes_ns;
+  lper = stage ? lper : lper_ns;
   const i64 lgrid = std::min<i64>((i64)num_sms() * std::max(lper, 1), p.count);
   const int sbytes = SW * kSolveRingFloats * (int)sizeof(float);
   if ((r = cuda_status(ensure_smem((const void*)mixed_solve_blocked_kernel<SW>, sbytes), name))) return r;
@@ -488,7 +496,7 @@ static int mixed_launch_blocked(MixedParams p, i64 kl_max, i64 ku_max, cudaStrea
   // counter[3] != 0: the first residual pass has work
   if ((r = cuda_status(cudaMemsetAsync(p.counter, 0, 4 * sizeof(int32_t), stream), name))) return r;
   if ((r = cuda_status(cudaMemsetAsync(reinterpret_cast<char*>(p.counter + 3), 1, 1, stream), name))) return r;
-  mixed_lu_blocked_kernel<<<(unsigned)lgrid, kBlkThreads, lbytes, stream>>>(p);
+  mixed_lu_blocked_kernel<<<(unsigned)lgrid, kBlkThreads, lbytes, stream>>>(p, stage ? 1 : 0);
   if ((r = launch_status(name))) return r;
   mixed_solve_blocked_kernel<SW><<<(unsigned)sgrid, 32 * SW, sbytes, stream>>>(p, 1, 1);  // queue counter[2]
   if ((r = launch_status(name))) return r;
@@ -598,7 +606,8 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
   if (p.count == 0) return BM_OK;
   const i64 kl_all = std::max(sc->n_wide > 0 ? sc->wide_kl : 0, sc->n_wide < p.count ? sc->narrow_kl : 0);
   const i64 ku_all = std::max(sc->n_wide > 0 ? sc->wide_ku : 0, sc->n_wide < p.count ? sc->narrow_ku : 0);
-  if (blk_lu_fits(kl_all, ku_all) && blk_solve_fits(kl_all, ku_all) && blk_smem_bytes(kl_all, ku_all) <= 227 * 1024)
+  if (blk_lu_fits(kl_all, ku_all) && blk_solve_fits(kl_all, ku_all) &&
+      blk_smem_bytes(kl_all, ku_all, false) <= 227 * 1024)
     return mixed_launch_blocked(p, kl_all, ku_all, stream, name);
   if (sc->warps == 8) return mixed_launch<8>(p, *sc, stream, name);
   return mixed_launch<4>(p, *sc, stream, name);

@@ -11,10 +11,10 @@
 //   shared memory as a ring in both dimensions (row i in slot i mod RR, column c in
 //   slot c mod CR), filled from the FP64 band and rounded on load.  Per panel of
 //   NB = 16 columns:
-//     1. warp 0 factors the panel in registers (one lane per row): idamax pivot
-//        (first largest |a|), interchange, scaling by the reciprocal pivot, rank-1
-//        update of the later panel columns; the interchanges are then replayed on the
-//        earlier L columns, as dgetrf's panel leaves them;
+//     1. warp 0 factors the panel in registers (one lane per row): partial pivot
+//        (largest |a|, one warp reduction), interchange, scaling by the reciprocal
+//        pivot, rank-1 update of the later panel columns; the interchanges are then
+//        replayed on the earlier L columns, as dgetrf's panel leaves them;
 //     2. every trailing column (one thread each) takes the panel's interchanges in
 //        order and the triangular solve U12 = L11^-1 A12 (16 rows, in registers);
 //     3. A22 -= L21 U12 by 4x4 register tiles (float4 shared-memory loads of L21);
@@ -22,7 +22,8 @@
 //        multipliers as step k left them, the layout gbtrs reads) and the U12 rows go
 //        to the FP32 factor storage;
 //     5. the window slides by 16 rows and columns; the elements it brings in are
-//        copied from the FP64 band with cp.async while steps 1-4 run.
+//        copied from the FP64 band with cp.async while steps 1-4 run (or, when the
+//        staging buffer would cost an SM a CTA, loaded at the slide).
 //   Zero pivots are skipped (no interchange, no scaling, no update) and reported in
 //   info, as dgbtf2 does.
 //
@@ -53,16 +54,16 @@ __host__ __device__ inline int blk_cr(int kl, int ku) { return kBlkNB + kl + ku;
 constexpr int kBlkHdrBytes = 128;
 // header, the FP32 window, and the FP64 staging of the elements the next slide brings
 // in (16 new rows over C columns, 16 new columns over kl rows)
-__host__ __device__ inline i64 blk_smem_bytes(i64 kl, i64 ku) {
+__host__ __device__ inline i64 blk_smem_bytes(i64 kl, i64 ku, bool stage = true) {
   return kBlkHdrBytes + (i64)blk_rs((int)kl) * blk_cr((int)kl, (int)ku) * 4 +
-         ((i64)blk_cr((int)kl, (int)ku) * kBlkNB + (i64)kBlkNB * kl) * 8;
+         (stage ? ((i64)blk_cr((int)kl, (int)ku) * kBlkNB + (i64)kBlkNB * kl) * 8 : 0);
 }
 
 // Factors system (n, kl, ku) from the FP64 band A (gbtrf storage: A(i,c) at row
 // kv + i - c, the matrix in rows kl..) into the FP32 storage A32 (same layout) and
 // ipiv (1-based).  Called by all kBlkThreads threads; returns info in every thread.
 __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i64 ldab, float* __restrict__ A32,
-                          i64 ldab32, i64* __restrict__ ipiv, unsigned char* smem) {
+                          i64 ldab32, i64* __restrict__ ipiv, unsigned char* smem, bool stage) {
   constexpr int NB = kBlkNB, NT = kBlkThreads;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int kv = kl + ku, R = NB + kl, RR = blk_rr(kl), RS = blk_rs(kl), C = NB + kv, CR = C;
@@ -128,7 +129,7 @@ __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i
   __syncthreads();
   for (i64 j0 = 0; j0 < n; j0 += NB) {
     const int jb = (int)min((i64)NB, n - j0);
-    if (j0 + jb < n) stage_slide(j0 + NB);
+    if (stage && j0 + jb < n) stage_slide(j0 + NB);
     // ---- 1. panel, by warp 0, in registers: lane L holds window rows L + 32k (k < 3)
     // of the panel's NB columns.  Step cc swaps rows cc and its pivot row in columns
     // cc.. only, so the L columns leave the panel as dgbtf2 leaves them (band storage
@@ -149,21 +150,22 @@ __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i
           const i64 j = j0 + cc;
           const int km = (int)min((i64)kl, n - 1 - j);
           bool inr[3];  // rows cc+1 .. cc+km (the multipliers' rows)
-          unsigned long long key = 0ull;
-          int idx = 0x7fffffff;
+          // Partial pivoting by one warp reduction: the key is |a| with its 7 low bits
+          // replaced by 127 - row, so the largest magnitude wins and, among magnitudes
+          // equal to 2^-16 relative, the first row (a stable pivot; the refinement
+          // does not need idamax's exact choice).  NaN keys never win.
+          unsigned key = 0u;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
             const int r = lane + 32 * k;
             inr[k] = r > cc && r <= cc + km;
             if (r >= cc && r <= cc + km) {
-              const unsigned long long kk = pivot_key(w[k][cc], r == cc);
-              if (idx == 0x7fffffff || kk > key) {
-                key = kk;
-                idx = r;
-              }
+              unsigned m = __float_as_uint(w[k][cc]) & 0x7fffffffu;
+              m = m > 0x7f800000u ? 0u : m;
+              key = max(key, (m & 0xffffff80u) | (unsigned)(127 - r));
             }
           }
-          const int p = warp_argmax_first(key, idx);  // pivot row (window index)
+          const int p = 127 - (int)(__reduce_max_sync(0xffffffffu, key) & 127u);  // pivot row (window index)
           const int pk = p >> 5, pl = p & 31;
           auto slot = [&](int c) { return pk == 0 ? w[0][c] : pk == 1 ? w[1][c] : w[2][c]; };
           const float pv = __shfl_sync(0xffffffffu, slot(cc), pl);
@@ -174,19 +176,24 @@ __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i
           }
           if (nz) {
             float u[NB];
+            if (p != cc) {
 #pragma unroll
-            for (int c = cc; c < NB; ++c) {
-              const float a = __shfl_sync(0xffffffffu, w[0][c], cc);  // row cc (lane cc, slot 0)
-              const float b = __shfl_sync(0xffffffffu, slot(c), pl);  // the pivot row
-              if (lane == cc) w[0][c] = b;
-              if (lane == pl && p != cc) {
-                if (pk == 0) w[0][c] = a;
-                else if (pk == 1) w[1][c] = a;
-                else w[2][c] = a;
+              for (int c = cc; c < NB; ++c) {
+                const float a = __shfl_sync(0xffffffffu, w[0][c], cc);  // row cc (lane cc, slot 0)
+                const float b = __shfl_sync(0xffffffffu, slot(c), pl);  // the pivot row
+                if (lane == cc) w[0][c] = b;
+                if (lane == pl) {
+                  if (pk == 0) w[0][c] = a;
+                  else if (pk == 1) w[1][c] = a;
+                  else w[2][c] = a;
+                }
+                u[c] = b;
               }
-              u[c] = b;
+            } else {  // no interchange: broadcast row cc
+#pragma unroll
+              for (int c = cc + 1; c < NB; ++c) u[c] = __shfl_sync(0xffffffffu, w[0][c], cc);
             }
-            const float rcp = 1.0f / pv;
+            const float rcp = __frcp_rn(pv);
 #pragma unroll
             for (int k = 0; k < 3; ++k)
               if (inr[k]) w[k][cc] *= rcp;
@@ -303,9 +310,9 @@ __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i
     __syncthreads();
     // ---- 5. slide by NB: new rows (old-frame R .. R+NB-1) over the new frame's columns,
     // new columns (old-frame C .. C+NB-1) over the retained rows
-    cp_async_wait<0>();
-    __syncthreads();
-    {
+    if (stage) {
+      cp_async_wait<0>();
+      __syncthreads();
       for (int e = tid; e < NB * C; e += NT) {
         const int c = e >> 4, rr = e & (NB - 1);  // new-frame column c, new row kl + rr
         W[cs(NB + c) * RS + rs(R + rr)] = (float)SR[e];
@@ -313,6 +320,38 @@ __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i
       for (int e = tid; e < NB * kl; e += NT) {
         const int cc = e / kl, r = e - cc * kl;  // new-frame column C-NB+cc, row r
         W[cs(C + cc) * RS + rs(NB + r)] = (float)SC[e];
+      }
+    } else {  // no staging buffer (more CTAs per SM): eight loads in flight per thread
+      const i64 nj = j0 + NB;
+      const int n1 = NB * C, tot = n1 + NB * kl;
+      for (int e0 = 0; e0 < tot; e0 += 8 * NT) {
+        float v[8];
+        int slot[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int e = e0 + q * NT + tid;
+          double a = 0.0;
+          slot[q] = -1;
+          if (e < tot) {
+            i64 i, col;
+            if (e < n1) {
+              const int c = e >> 4, rr = e & (NB - 1);
+              i = nj + kl + rr;
+              col = nj + c;
+              slot[q] = cs(NB + c) * RS + rs(R + rr);
+            } else {
+              const int f = e - n1, cc = f / kl, r = f - cc * kl;
+              i = nj + r;
+              col = nj + C - NB + cc;
+              slot[q] = cs(C + cc) * RS + rs(NB + r);
+            }
+            if (inband(i, col)) a = A[(kv + i - col) + col * ldab];
+          }
+          v[q] = (float)a;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (slot[q] >= 0) W[slot[q]] = v[q];
       }
     }
     __syncthreads();
