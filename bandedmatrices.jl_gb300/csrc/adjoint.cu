@@ -1,5 +1,5 @@
 // Adjoint of the banded solve X = A \ B (no counterpart in the reference; the
-// rrule the benchmark spec adds beside ldiv!, src/banded/linalg.jl:24-47).
+// ChainRules rrule of \ built beside ldiv!, src/banded/linalg.jl:24-47).
 //
 // For a loss L with upstream gradient W = dL/dX:
 //     dL/dB = A^{-T} W                  (xGBTRS 'T' on the stored factors -- the

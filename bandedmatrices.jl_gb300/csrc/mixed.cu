@@ -1,5 +1,5 @@
-// Mixed-precision refined banded solves (no counterpart in the reference; the
-// spec addition beside lu!/ldiv!, src/banded/BandedLU.jl:90-103,
+// Mixed-precision refined banded solves (no counterpart in the reference; an
+// addition beside lu!/ldiv!, src/banded/BandedLU.jl:90-103,
 // src/banded/linalg.jl:24-30).
 //
 // Per system s the FP64 band A is rounded to an FP32 copy in gbtrf storage and

@@ -404,7 +404,7 @@ int P##gbqr_lmul(char trans, i64 m, i64 n, i64 l, i64 u, const T *D, i64 ldd, co
 DEFINE_ALL(double, or_d, fma, fabs, sqrt, copysign)
 DEFINE_ALL(float, or_s, fmaf, fabsf, sqrtf, copysignf)
 
-/* Adjoint of x = A \ b with L = w.x (the spec rrule): lambda = A^{-T} w via the
+/* Adjoint of x = A \ b with L = w.x (the rrule of \): lambda = A^{-T} w via the
  * transposed xGBTRS on the stored factors; dL/db = lambda; dL/dA(i,j) = -lambda_i x_j on
  * the band of A (BLAS band storage, (kl+ku+1) x n, leading dim ldg). */
 int or_dgb_adjoint(i64 n, i64 kl, i64 ku, const double *lu, i64 ldab, const i64 *ipiv,
