@@ -1,0 +1,100 @@
+"""Host-side logic of the Python mirror, on CPU tensors: band storage layout and the
+BandedMatrix constructors (src/banded/BandedMatrix.jl:16-68, 222-232), the PDE operator
+assembly, and the batched solver's longest-first schedules.  No GPU and no library call."""
+import numpy as np
+import pytest
+import torch
+
+
+def _dense_band(rng, m, n, l, u):
+    A = np.zeros((m, n))
+    for j in range(n):
+        for i in range(max(0, j - u), min(m, j + l + 1)):
+            A[i, j] = rng.standard_normal()
+    return A
+
+
+@pytest.mark.parametrize("m,n,l,u", [(7, 7, 2, 1), (9, 5, 3, 0), (5, 9, 0, 4), (6, 6, 0, 0), (4, 10, 1, 6)])
+def test_band_storage_round_trip(bm, m, n, l, u):
+    rng = np.random.default_rng(m * 100 + n * 10 + l + u)
+    A = torch.from_numpy(_dense_band(rng, m, n, l, u))
+    B = bm.BandedMatrix.from_dense(A, (l, u))
+    assert B.shape == (m, n) and bm.bandwidths(B) == (l, u)
+    assert B.data.shape == (l + u + 1, n) and B.data.stride(0) == 1 and B.lda >= l + u + 1
+    # A[k, j] = data[u + k - j, j] (src/banded/BandedMatrix.jl:414-419)
+    for j in range(n):
+        for k in range(max(0, j - u), min(m, j + l + 1)):
+            assert B.data[u + k - j, j].item() == A[k, j].item()
+    assert torch.equal(B.to_dense(), A)
+    W = B.rewiden((l + 2, u + 1))
+    assert bm.bandwidths(W) == (l + 2, u + 1) and torch.equal(W.to_dense(), A)
+    with pytest.raises(Exception):
+        B.rewiden((max(l - 1, 0) if l else -1, u))
+
+
+def test_band_storage_with_padding(bm):
+    d = bm.band_storage(3, 6, torch.float64, "cpu", lda=5, fill=0.0)
+    assert d.shape == (3, 6) and d.stride() == (1, 5)
+    B = bm.BandedMatrix(d, 6, 1, 1)
+    assert B.lda == 5
+
+
+def test_diffusion_operator_assembly(bm):
+    """The 5-point variable-coefficient operator in natural ordering (harmonic face means,
+    boundary faces taking the cell value) against a cell-by-cell dense assembly."""
+    G = 5
+    kc = np.exp(bm.pde.gaussian_field(G, 2.0, seed=3))
+    A = bm.pde.diffusion_band(kc, torch.float64, "cpu")
+    assert A.shape == (G * G, G * G) and bm.bandwidths(A) == (G, G)
+    D = np.zeros((G * G, G * G))
+    hm = lambda a, b: 2 * a * b / (a + b)
+    for i in range(G):
+        for j in range(G):
+            p = i * G + j
+            for di, dj in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+                ii, jj = i + di, j + dj
+                if 0 <= ii < G and 0 <= jj < G:
+                    f = hm(kc[i, j], kc[ii, jj])
+                    D[p, ii * G + jj] = -f
+                    D[p, p] += f
+                else:
+                    D[p, p] += kc[i, j]
+    Ad = A.to_dense().numpy()
+    assert np.allclose(Ad, D, rtol=1e-14, atol=0)
+    assert np.array_equal(Ad, Ad.T)
+    # weakly diagonally dominant; strictly on the boundary cells (their outer faces)
+    off = np.abs(Ad).sum(1) - np.diag(Ad)
+    assert (np.diag(Ad) >= off * (1 - 1e-14)).all()
+    edge = np.zeros((G, G), bool)
+    edge[0, :] = edge[-1, :] = edge[:, 0] = edge[:, -1] = True
+    assert (np.diag(Ad)[edge.ravel()] > off[edge.ravel()]).all()
+
+
+def test_gaussian_field_is_seeded_and_normalised(bm):
+    g1 = bm.pde.gaussian_field(64, 16.0, seed=11)
+    g2 = bm.pde.gaussian_field(64, 16.0, seed=11)
+    assert np.array_equal(g1, g2)
+    assert abs(g1.mean()) < 1e-12 and abs(g1.std() - 1.0) < 1e-12
+    # correlation length 16 cells: neighbours are strongly correlated
+    assert np.corrcoef(g1[:, :-1].ravel(), g1[:, 1:].ravel())[0, 1] > 0.9
+
+
+def test_longest_first_orders(bm):
+    from importlib import import_module
+
+    batched = import_module(bm.__name__ + ".batched")
+    rng = np.random.default_rng(5)
+    n = rng.integers(10, 2000, 300)
+    kl = rng.integers(0, 40, 300)
+    ku = rng.integers(0, 40, 300)
+    nrhs = rng.integers(1, 9, 300)
+    cost = n * (2 * kl * (kl + ku) + kl) + nrhs * 2 * n * (2 * kl + ku + 1)
+    order = batched.lpt_order(n, kl, ku, nrhs)
+    assert sorted(order.tolist()) == list(range(300))
+    assert (np.diff(cost[order]) <= 0).all()
+    order2, n_wide = batched.schedule_order(n, kl, ku, nrhs, narrow_cols=24)
+    assert sorted(order2.tolist()) == list(range(300))
+    wide = (kl + ku + 1) > 24
+    assert n_wide == int(wide.sum())
+    assert wide[order2[:n_wide]].all() and not wide[order2[n_wide:]].any()
+    assert (np.diff(cost[order2[:n_wide]]) <= 0).all() and (np.diff(cost[order2[n_wide:]]) <= 0).all()
