@@ -27,8 +27,9 @@
 //   Zero pivots are skipped (no interchange, no scaling, no update) and reported in
 //   info, as dgbtf2 does.
 //
-// blk_solve_warp -- one warp solves up to 4 right-hand sides of a system: lane l keeps rows i = l (mod 32) of the window in registers (a ring of NS
-//   slots per right-hand side).  Forward sweep (dgbtrs 'N'): interchange b(j) with
+// blk_solve_warp -- one warp solves up to 4 right-hand sides of a system: lane l
+//   keeps rows i = l (mod 32) of the window in registers (a ring of NS slots per
+//   right-hand side).  Forward sweep (dgbtrs 'N'): interchange b(j) with
 //   b(ipiv(j)) by two shuffles, then b(j+1 .. j+kl) -= L(:, j) b(j), one fma per lane
 //   and slot.  Back substitution (U, bandwidth kv): x(j) = b(j) * (1 / U(j,j)), then
 //   b(j-kv .. j-1) -= U(:, j) x(j).  The step's L or U column is read from the factor
