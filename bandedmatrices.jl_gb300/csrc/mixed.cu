@@ -615,36 +615,70 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
 
 }  // namespace bm
 
+// Arguments are checked in order, LAPACK style (-i for argument i), before any CUDA
+// call; `order` may be NULL (natural order).
 extern "C" int bm_dsgbsv_batched(int64_t count, const bm_gb_desc* descs, const int32_t* order, const double* AB,
                                  const double* B, double* X, int64_t* ipiv, int64_t* info, float* AB32, float* R32,
                                  int32_t* iters, double* berr, int32_t* counter, double tol, int64_t maxit,
                                  int64_t max_kl, int64_t max_ku, bm_stream_t stream) {
+  if (count < 0) return -1;
+  if (count > 0) {
+    if (!descs) return -2;
+    if (!AB) return -4;
+    if (!B) return -5;
+    if (!X) return -6;
+    if (!ipiv) return -7;
+    if (!info) return -8;
+    if (!AB32) return -9;
+    if (!R32) return -10;
+    if (!iters) return -11;
+    if (!berr) return -12;
+  }
+  if (!counter) return -13;
+  if (!(tol >= 0.0)) return -14;
+  if (maxit < 0) return -15;
+  if (max_kl < 0) return -16;
+  if (max_ku < 0) return -17;
   bm::MixedParams p;
   p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
   p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
   p.maxit = (int)std::min<int64_t>(maxit, bm::kMixedMaxCorrections);
   p.group_elems = 0;
-  if (maxit < 0) return -15;
-  if (max_kl < 0) return -17;
-  if (max_ku < 0) return -18;
   bm_gb_schedule sc;  // every system wide (4 warps) once the widest window holds 512 entries, else narrow
   sc.n_wide = (max_kl + 1) * (max_kl + max_ku + 1) >= 512 ? count : 0;
   sc.warps = 4;
   sc.wide_kl = sc.narrow_kl = max_kl;
   sc.wide_ku = sc.narrow_ku = max_ku;
-  const int r = bm::dsgbsv_batched_impl(p, &sc, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched");
-  return r == -4 ? -17 : r;
+  return bm::dsgbsv_batched_impl(p, &sc, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched");
 }
 
 extern "C" int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, const int32_t* order,
                                        const bm_gb_schedule* sched, const double* AB, const double* B, double* X,
                                        int64_t* ipiv, int64_t* info, float* AB32, float* R32, int32_t* iters,
                                        double* berr, int32_t* counter, double tol, int64_t maxit, bm_stream_t stream) {
+  if (count < 0) return -1;
+  if (count > 0 && !descs) return -2;
+  if (!sched || sched->n_wide < 0 || sched->n_wide > count || (sched->warps != 4 && sched->warps != 8) ||
+      sched->wide_kl < 0 || sched->wide_ku < 0 || sched->narrow_kl < 0 || sched->narrow_ku < 0)
+    return -4;
+  if (count > 0) {
+    if (!AB) return -5;
+    if (!B) return -6;
+    if (!X) return -7;
+    if (!ipiv) return -8;
+    if (!info) return -9;
+    if (!AB32) return -10;
+    if (!R32) return -11;
+    if (!iters) return -12;
+    if (!berr) return -13;
+  }
+  if (!counter) return -14;
+  if (!(tol >= 0.0)) return -15;
+  if (maxit < 0) return -16;
   bm::MixedParams p;
   p.count = count; p.descs = descs; p.order = order; p.AB = AB; p.B = B; p.X = X; p.ipiv = ipiv; p.info = info;
   p.AB32 = AB32; p.R32 = R32; p.iters = iters; p.berr = berr; p.counter = counter; p.tol = tol;
   p.maxit = (int)std::min<int64_t>(maxit, bm::kMixedMaxCorrections);
   p.group_elems = 0;
-  if (maxit < 0) return -16;
   return bm::dsgbsv_batched_impl(p, sched, reinterpret_cast<cudaStream_t>(stream), "bm_dsgbsv_batched_sched");
 }

@@ -38,3 +38,63 @@ def test_library_reports_version_without_gpu(bm):
     L = bm._lib.load()
     assert L.bm_version() >= 100
     assert isinstance(L.bm_last_error(), bytes)
+
+
+def test_illegal_arguments_are_reported_before_any_device_call(bm):
+    """LAPACK-style status (-i for the first illegal argument i), decided on the host, so
+    it needs no GPU: the xGBMV / xGBTRF / xGBTRS checks the reference's LAPACK performs,
+    and the refined batched solve's pointer, tolerance and bandwidth checks."""
+    L = bm._lib.load()
+    P = ctypes.c_void_p
+    fake = P(256)  # never dereferenced: every call below stops at an argument check
+    s = P(0)
+    # xgbmv(trans, m, n, kl, ku, alpha, A, lda, x, incx, beta, y, incy, stream)
+    gbmv = lambda *a: L.bm_dgbmv(*a)
+    assert gbmv(b"X", 4, 4, 1, 1, 1.0, fake, 3, fake, 1, 0.0, fake, 1, s) == -1
+    assert gbmv(b"N", -1, 4, 1, 1, 1.0, fake, 3, fake, 1, 0.0, fake, 1, s) == -2
+    assert gbmv(b"N", 4, -1, 1, 1, 1.0, fake, 3, fake, 1, 0.0, fake, 1, s) == -3
+    assert gbmv(b"N", 4, 4, -1, 1, 1.0, fake, 3, fake, 1, 0.0, fake, 1, s) == -4
+    assert gbmv(b"N", 4, 4, 1, 1, 1.0, fake, 2, fake, 1, 0.0, fake, 1, s) == -8
+    assert gbmv(b"T", 4, 4, 1, 1, 1.0, fake, 3, fake, 0, 0.0, fake, 1, s) == -10
+    assert gbmv(b"N", 4, 4, 1, 1, 1.0, fake, 3, fake, 1, 0.0, fake, 0, s) == -13
+    # xgbtrf(m, n, kl, ku, AB, ldab, ipiv, info, stream)
+    assert L.bm_dgbtrf(-1, 4, 1, 1, fake, 4, fake, fake, s) == -1
+    assert L.bm_dgbtrf(4, -1, 1, 1, fake, 4, fake, fake, s) == -2
+    assert L.bm_dgbtrf(4, 4, -1, 1, fake, 4, fake, fake, s) == -3
+    assert L.bm_dgbtrf(4, 4, 1, -1, fake, 4, fake, fake, s) == -4
+    assert L.bm_sgbtrf(4, 4, 1, 1, fake, 3, fake, fake, s) == -6  # ldab < 2kl+ku+1
+    # xgbtrs(trans, n, kl, ku, nrhs, AB, ldab, ipiv, B, ldb, stream)
+    assert L.bm_dgbtrs(b"Q", 4, 1, 1, 1, fake, 4, fake, fake, 4, s) == -1
+    assert L.bm_dgbtrs(b"N", -1, 1, 1, 1, fake, 4, fake, fake, 4, s) == -2
+    assert L.bm_dgbtrs(b"N", 4, 1, 1, -1, fake, 4, fake, fake, 4, s) == -5
+    assert L.bm_dgbtrs(b"T", 4, 1, 1, 1, fake, 3, fake, fake, 4, s) == -7
+    assert L.bm_dgbtrs(b"N", 4, 1, 1, 1, fake, 4, fake, fake, 3, s) == -10
+    # refined batched solve: (count, descs, order, AB, B, X, ipiv, info, AB32, R32, iters,
+    # berr, counter, tol, maxit, max_kl, max_ku, stream)
+    ok = [fake] * 12
+
+    def ds(count=1, ptrs=None, counter=fake, tol=1e-10, maxit=30, max_kl=2, max_ku=2):
+        p = list(ptrs or ok)
+        return L.bm_dsgbsv_batched(count, p[0], None, *p[2:11], counter, tol, maxit, max_kl, max_ku, s)
+
+    assert ds(count=-1) == -1
+    for arg, idx in ((2, 0), (4, 2), (5, 3), (6, 4), (7, 5), (8, 6), (9, 7), (10, 8), (11, 9), (12, 10)):
+        p = list(ok)
+        p[idx] = None
+        assert ds(ptrs=p) == -arg, arg
+    assert ds(counter=None) == -13
+    assert ds(tol=float("nan")) == -14
+    assert ds(maxit=-1) == -15
+    assert ds(max_kl=-1) == -16
+    assert ds(max_ku=-1) == -17
+    assert ds(count=0, ptrs=[None] * 12) == 0  # an empty batch: nothing to enqueue
+    # the schedule form checks its schedule as argument 4 and shifts the rest by one
+    from importlib import import_module
+
+    Schedule = import_module(bm.__name__ + ".batched").Schedule
+    good, bad = Schedule(1, 4, 2, 2, 2, 2), Schedule(1, 3, 2, 2, 2, 2)
+    dss = lambda sch, counter=fake, tol=1e-10: L.bm_dsgbsv_batched_sched(
+        1, fake, None, ctypes.byref(sch), *([fake] * 9), counter, tol, 30, s)
+    assert dss(bad) == -4
+    assert dss(good, counter=None) == -14
+    assert dss(good, tol=-1.0) == -15
