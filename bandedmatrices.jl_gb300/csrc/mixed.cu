@@ -616,21 +616,16 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
 }  // namespace bm
 
 // Arguments are checked in order, LAPACK style (-i for argument i), before any CUDA
-// call; `order` may be NULL (natural order).
+// call; `order` may be NULL (natural order), and the band, right-hand-side and pivot
+// buffers may be NULL when they are empty.
 extern "C" int bm_dsgbsv_batched(int64_t count, const bm_gb_desc* descs, const int32_t* order, const double* AB,
                                  const double* B, double* X, int64_t* ipiv, int64_t* info, float* AB32, float* R32,
                                  int32_t* iters, double* berr, int32_t* counter, double tol, int64_t maxit,
                                  int64_t max_kl, int64_t max_ku, bm_stream_t stream) {
   if (count < 0) return -1;
-  if (count > 0) {
+  if (count > 0) {  // the per-system arrays (the others may be empty: all n or nrhs zero)
     if (!descs) return -2;
-    if (!AB) return -4;
-    if (!B) return -5;
-    if (!X) return -6;
-    if (!ipiv) return -7;
     if (!info) return -8;
-    if (!AB32) return -9;
-    if (!R32) return -10;
     if (!iters) return -11;
     if (!berr) return -12;
   }
@@ -661,14 +656,8 @@ extern "C" int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc* descs, c
   if (!sched || sched->n_wide < 0 || sched->n_wide > count || (sched->warps != 4 && sched->warps != 8) ||
       sched->wide_kl < 0 || sched->wide_ku < 0 || sched->narrow_kl < 0 || sched->narrow_ku < 0)
     return -4;
-  if (count > 0) {
-    if (!AB) return -5;
-    if (!B) return -6;
-    if (!X) return -7;
-    if (!ipiv) return -8;
+  if (count > 0) {  // the per-system arrays (the others may be empty: all n or nrhs zero)
     if (!info) return -9;
-    if (!AB32) return -10;
-    if (!R32) return -11;
     if (!iters) return -12;
     if (!berr) return -13;
   }

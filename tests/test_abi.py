@@ -43,7 +43,7 @@ def test_library_reports_version_without_gpu(bm):
 def test_illegal_arguments_are_reported_before_any_device_call(bm):
     """LAPACK-style status (-i for the first illegal argument i), decided on the host, so
     it needs no GPU: the xGBMV / xGBTRF / xGBTRS checks the reference's LAPACK performs,
-    and the refined batched solve's pointer, tolerance and bandwidth checks."""
+    and the refined batched solve's per-system pointer, tolerance and bandwidth checks."""
     L = bm._lib.load()
     P = ctypes.c_void_p
     fake = P(256)  # never dereferenced: every call below stops at an argument check
@@ -78,7 +78,7 @@ def test_illegal_arguments_are_reported_before_any_device_call(bm):
         return L.bm_dsgbsv_batched(count, p[0], None, *p[2:11], counter, tol, maxit, max_kl, max_ku, s)
 
     assert ds(count=-1) == -1
-    for arg, idx in ((2, 0), (4, 2), (5, 3), (6, 4), (7, 5), (8, 6), (9, 7), (10, 8), (11, 9), (12, 10)):
+    for arg, idx in ((2, 0), (8, 6), (11, 9), (12, 10)):  # descs, info, iters, berr
         p = list(ok)
         p[idx] = None
         assert ds(ptrs=p) == -arg, arg
@@ -88,6 +88,10 @@ def test_illegal_arguments_are_reported_before_any_device_call(bm):
     assert ds(max_kl=-1) == -16
     assert ds(max_ku=-1) == -17
     assert ds(count=0, ptrs=[None] * 12) == 0  # an empty batch: nothing to enqueue
+    # empty buffers may be NULL (every system with n = 0 or nrhs = 0), not the per-system ones
+    p = list(ok)
+    p[2] = p[3] = p[4] = p[5] = p[7] = p[8] = None
+    assert ds(ptrs=p, counter=None) == -13  # reached the counter check
     # the schedule form checks its schedule as argument 4 and shifts the rest by one
     from importlib import import_module
 
