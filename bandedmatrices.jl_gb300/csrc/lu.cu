@@ -479,6 +479,7 @@ static int gbsv_batched_sched_impl(i64 count, const bm_gb_desc* descs, const int
   if (sc->n_wide < 0 || sc->n_wide > count || (sc->warps != 4 && sc->warps != 8) || sc->wide_kl < 0 ||
       sc->wide_ku < 0 || sc->narrow_kl < 0 || sc->narrow_ku < 0)
     return -4;
+  if (!info && count) return -8;
   if (!counter) return -9;
   if (count == 0) return BM_OK;
   if (sc->warps == 8) return gbsv_batched_launch<T, 8>(count, descs, order, *sc, AB, ipiv, B, info, counter, stream, name);
@@ -500,11 +501,16 @@ template <typename T>
 static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* order, T* AB, i64* ipiv, T* B,
                              i64* info, int32_t* counter, i64 max_kl, i64 max_ku, cudaStream_t stream,
                              const char* name) {
-  if (max_kl < 0) return -10;
-  if (max_ku < 0) return -11;
+  // arguments in order (count 1, descs 2, order 3, AB 4, ipiv 5, B 6, info 7, counter 8,
+  // max_kl 9, max_ku 10); the schedule built from them is then always valid
+  if (count < 0) return -1;
+  if (!descs && count) return -2;
+  if (!info && count) return -7;
+  if (!counter) return -8;
+  if (max_kl < 0) return -9;
+  if (max_ku < 0) return -10;
   const bm_gb_schedule sc = default_schedule(count, max_kl, max_ku);
-  const int r = gbsv_batched_sched_impl<T>(count, descs, order, &sc, AB, ipiv, B, info, counter, stream, name);
-  return r == -4 ? -10 : r;
+  return gbsv_batched_sched_impl<T>(count, descs, order, &sc, AB, ipiv, B, info, counter, stream, name);
 }
 
 // ---------------------------------------------------------------------------
@@ -576,6 +582,7 @@ static int gbsv_batched_noalloc_impl(i64 count, const bm_gb_desc* descs, double*
                                      i64 max_kl, i64 max_ku, cudaStream_t stream, const char* name) {
   if (count < 0) return -1;
   if (!descs && count) return -2;
+  if (!info && count) return -6;
   if (max_kl < 0) return -7;
   if (max_ku < 0) return -8;
   if (count > kNoAllocMaxSystems) {

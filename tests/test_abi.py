@@ -102,3 +102,34 @@ def test_illegal_arguments_are_reported_before_any_device_call(bm):
     assert dss(bad) == -4
     assert dss(good, counter=None) == -14
     assert dss(good, tol=-1.0) == -15
+
+
+def test_batched_argument_codes_without_gpu(bm):
+    """The plain batched entry points report their first illegal argument by position."""
+    L = bm._lib.load()
+    P = ctypes.c_void_p
+    fake, s = P(256), P(0)
+    # bm_dgbsv_batched(count, descs, order, AB, ipiv, B, info, counter, max_kl, max_ku, stream)
+    b = lambda count=1, descs=fake, info=fake, counter=fake, kl=2, ku=2: L.bm_dgbsv_batched(
+        count, descs, None, fake, fake, fake, info, counter, kl, ku, s)
+    assert b(count=-1) == -1
+    assert b(descs=None) == -2
+    assert b(info=None) == -7
+    assert b(counter=None) == -8
+    assert b(kl=-1) == -9
+    assert b(ku=-1) == -10
+    assert b(count=0, descs=None, info=None) == 0
+    # the schedule form: (count, descs, order, sched, AB, ipiv, B, info, counter, stream)
+    from importlib import import_module
+
+    Schedule = import_module(bm.__name__ + ".batched").Schedule
+    good, bad = Schedule(1, 4, 2, 2, 2, 2), Schedule(2, 4, 2, 2, 2, 2)  # bad: n_wide > count
+    bs = lambda sch, info=fake, counter=fake: L.bm_sgbsv_batched_sched(
+        1, fake, None, ctypes.byref(sch), fake, fake, fake, info, counter, s)
+    assert bs(bad) == -4
+    assert bs(good, info=None) == -8
+    assert bs(good, counter=None) == -9
+    # the allocation-free form: (count, descs, AB, ipiv, B, info, max_kl, max_ku, stream)
+    assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, None, 2, 2, s) == -6
+    assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, fake, -1, 2, s) == -7
+    assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, fake, 2, -1, s) == -8
