@@ -133,3 +133,41 @@ def test_batched_argument_codes_without_gpu(bm):
     assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, None, 2, 2, s) == -6
     assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, fake, -1, 2, s) == -7
     assert L.bm_dgbsv_batched_noalloc(1, fake, fake, fake, fake, fake, 2, -1, s) == -8
+
+
+def test_product_qr_triangular_and_adjoint_codes_without_gpu(bm):
+    """gbmm (src/banded/gbmm.jl:207: C must hold the product's bands), banded QR and its
+    Q application, tbsv and the adjoint report their first illegal argument by position."""
+    L = bm._lib.load()
+    P = ctypes.c_void_p
+    f, s = P(256), P(0)
+    # gbmm(n, nu, m, Al, Au, Bl, Bu, Cl, Cu, alpha, A, lda, B, ldb, beta, C, ldc, stream)
+    g = lambda *a: L.bm_dgbmm(*a[:9], 1.0, f, a[9], f, a[10], 0.0, f, a[11], s)
+    assert g(-1, 8, 8, 1, 1, 1, 1, 2, 2, 3, 3, 5) == -1
+    assert g(8, 8, 8, 1, -1, 1, 1, 2, 2, 3, 3, 5) == -5
+    assert g(8, 8, 8, 1, 1, 1, 1, 1, 2, 3, 3, 5) == -8  # Cl < Al + Bl
+    assert g(8, 8, 8, 1, 1, 1, 1, 2, 1, 3, 3, 5) == -9  # Cu < Au + Bu
+    assert g(8, 8, 8, 1, 1, 1, 1, 2, 2, 2, 3, 5) == -12
+    assert g(8, 8, 8, 1, 1, 1, 1, 2, 2, 3, 2, 5) == -14
+    assert g(8, 8, 8, 1, 1, 1, 1, 2, 2, 3, 3, 4) == -17
+    # gbqrf(m, n, l, u, AB, ldab, tau, stream); gbqr_lmul(trans, m, n, l, u, AB, ldab, tau,
+    # ntau, nrhs, B, ldb, stream); tbsv(uplo, trans, diag, n, k, A, lda, x, incx, stream)
+    assert L.bm_dgbqrf(8, 8, -1, 2, f, 6, f, s) == -3
+    assert L.bm_dgbqrf(8, 8, 1, 2, f, 3, f, s) == -6
+    assert L.bm_dgbqrf(8, 8, 1, 2, f, 6, None, s) == -7
+    assert L.bm_dgbqr_lmul(b"X", 8, 8, 1, 2, f, 6, f, 8, 1, f, 8, s) == -1
+    assert L.bm_dgbqr_lmul(b"T", 8, 8, 1, 2, f, 6, f, -1, 1, f, 8, s) == -9
+    assert L.bm_dgbqr_lmul(b"N", 8, 8, 1, 2, f, 6, f, 8, 1, f, 7, s) == -12
+    assert L.bm_dtbsv(b"X", b"N", b"N", 8, 2, f, 3, f, 1, s) == -1
+    assert L.bm_dtbsv(b"U", b"X", b"N", 8, 2, f, 3, f, 1, s) == -2
+    assert L.bm_dtbsv(b"U", b"N", b"X", 8, 2, f, 3, f, 1, s) == -3
+    assert L.bm_dtbsv(b"U", b"N", b"N", 8, 2, f, 2, f, 1, s) == -7
+    assert L.bm_dtbsv(b"U", b"T", b"N", 8, 2, f, 3, f, 0, s) == -9
+    # adjoint(n, kl, ku, nrhs, LU, ldab, ipiv, X, B, W, grad_B, grad_band, ldg, Xwork, stream)
+    adj = lambda n=8, nrhs=1, ldab=6, X=f, B=f, ldg=4, Xw=f: L.bm_dgbsv_adjoint(
+        n, 2, 1, nrhs, f, ldab, f, X, B, f, f, f, ldg, Xw, s)
+    assert adj(n=-1) == -1
+    assert adj(nrhs=-1) == -4
+    assert adj(ldab=5) == -6
+    assert adj(X=None, Xw=None) == -8  # X not kept and no workspace to recompute it in
+    assert adj(ldg=3) == -13
