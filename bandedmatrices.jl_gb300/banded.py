@@ -155,6 +155,32 @@ class BandedMatrix:
         d[u2 - self.u: u2 - self.u + self.l + self.u + 1, :] = self.data
         return BandedMatrix(d, self.m, l2, u2)
 
+    # -- scalar indexing (0-based k, j; the reference's A[k+1, j+1]) -----------
+    def _checkbounds(self, k: int, j: int) -> None:
+        if not (0 <= k < self.m and 0 <= j < self.n):
+            raise IndexError(f"index ({k}, {j}) is out of bounds for a {self.m}x{self.n} BandedMatrix")
+
+    def __getitem__(self, idx):
+        """A[k, j]: the band entry data[u + k - j, j], zero outside the band
+        (banded_getindex / inbands_getindex, src/banded/BandedMatrix.jl:414-442).  Reads
+        one element from the device: a diagnostic, not a hot path."""
+        k, j = (int(i) for i in idx)
+        self._checkbounds(k, j)
+        if -self.l <= j - k <= self.u:
+            return self.data[self.u + k - j, j].item()
+        return 0.0
+
+    def __setitem__(self, idx, v) -> None:
+        """A[k, j] = v: writes the band entry; outside the band only v == 0 is accepted
+        and BandError is raised otherwise (banded_setindex!,
+        src/banded/BandedMatrix.jl:627-643)."""
+        k, j = (int(i) for i in idx)
+        self._checkbounds(k, j)
+        if -self.l <= j - k <= self.u:
+            self.data[self.u + k - j, j] = v
+        elif v != 0:
+            raise BandError(f"cannot set band {j - k} of a BandedMatrix with bandwidths ({self.l}, {self.u})")
+
     # -- operators -----------------------------------------------------------
     def __matmul__(self, other):
         from . import linalg

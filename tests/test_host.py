@@ -98,3 +98,27 @@ def test_longest_first_orders(bm):
     assert n_wide == int(wide.sum())
     assert wide[order2[:n_wide]].all() and not wide[order2[n_wide:]].any()
     assert (np.diff(cost[order2[:n_wide]]) <= 0).all() and (np.diff(cost[order2[n_wide:]]) <= 0).all()
+
+
+def test_scalar_indexing_semantics(bm):
+    """A[k, j] reads the band entry or zero outside the band; A[k, j] = v writes in-band
+    entries, accepts zero outside the band and raises BandError otherwise
+    (src/banded/BandedMatrix.jl:414-442, 627-643); out-of-range indices raise IndexError."""
+    rng = np.random.default_rng(9)
+    m, n, l, u = 7, 6, 2, 1
+    Ad = _dense_band(rng, m, n, l, u)
+    A = bm.BandedMatrix.from_dense(torch.from_numpy(Ad), (l, u))
+    for k in range(m):
+        for j in range(n):
+            assert A[k, j] == Ad[k, j]
+    A[3, 2] = 5.0  # in band (j - k = -1)
+    assert A[3, 2] == 5.0 and A.data[u + 3 - 2, 2].item() == 5.0
+    A[0, 5] = 0.0  # outside the band, zero: accepted, nothing stored
+    with pytest.raises(bm.BandError):
+        A[0, 5] = 1.0
+    with pytest.raises(bm.BandError):
+        A[6, 0] = -2.0
+    with pytest.raises(IndexError):
+        A[7, 0]
+    with pytest.raises(IndexError):
+        A[0, -1] = 0.0
