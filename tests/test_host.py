@@ -122,3 +122,20 @@ def test_scalar_indexing_semantics(bm):
         A[7, 0]
     with pytest.raises(IndexError):
         A[0, -1] = 0.0
+
+
+def test_random_constructors_and_bandwidth(bm):
+    """brand fills every storage slot, the off-matrix corners included, from [0, 1); brandn
+    from the standard normal (src/banded/BandedMatrix.jl:184-204); bandwidth(A, 1) = l,
+    bandwidth(A, 2) = u."""
+    g = torch.Generator().manual_seed(4)
+    A = bm.brand(torch.float64, 300, 200, 3, 5, device="cpu", generator=g)
+    assert A.shape == (300, 200) and bm.bandwidths(A) == (3, 5)
+    assert bm.bandwidth(A, 1) == 3 and bm.bandwidth(A, 2) == 5
+    d = bm.bandeddata(A)
+    assert d.shape == (9, 200) and bool((d >= 0).all()) and bool((d < 1).all())
+    assert abs(d.mean().item() - 0.5) < 0.02
+    B = bm.brandn(torch.float32, 200, 200, 2, 2, device="cpu", generator=g)
+    assert B.dtype == torch.float32 and abs(B.data.mean().item()) < 0.05 and abs(B.data.std().item() - 1) < 0.05
+    Z = bm.BandedMatrix.zeros((5, 4), (1, 2), torch.float64, "cpu")
+    assert torch.equal(Z.to_dense(), torch.zeros(5, 4, dtype=torch.float64))
