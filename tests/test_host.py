@@ -139,3 +139,27 @@ def test_random_constructors_and_bandwidth(bm):
     assert B.dtype == torch.float32 and abs(B.data.mean().item()) < 0.05 and abs(B.data.std().item() - 1) < 0.05
     Z = bm.BandedMatrix.zeros((5, 4), (1, 2), torch.float64, "cpu")
     assert torch.equal(Z.to_dense(), torch.zeros(5, 4, dtype=torch.float64))
+
+
+@pytest.mark.parametrize("n,l,u", [(40, 3, 2), (25, 0, 4), (30, 5, 0), (12, 11, 11)])
+def test_banded_lu_views(bm, orc, n, l, u):
+    """BandedLU's p, L and U views (src/banded/BandedLU.jl:114-130) rebuilt from gbtrf
+    factors and pivots (here the oracle's xGBTF2 on a non-dominant band, so rows are
+    interchanged): A[p, :] == L U, L unit lower triangular, U upper triangular with
+    bandwidth l + u."""
+    from importlib import import_module
+
+    lu_mod = import_module(bm.__name__ + ".lu")
+    rng = np.random.default_rng(n * 7 + l + u)
+    data = rng.standard_normal((l + u + 1, n))
+    LU, ipiv, info = orc.gbtf2(n, n, l, u, orc.lu_storage(data, n, l, u))
+    assert info == 0 and (ipiv != np.arange(1, n + 1)).any() or l == 0
+    F = lu_mod.BandedLU(bm.BandedMatrix(torch.from_numpy(np.ascontiguousarray(LU.T)).t(), n, l, l + u),
+                        torch.from_numpy(ipiv), torch.tensor([info]), l, u)
+    A = orc.band_to_dense(data, n, l, u)
+    Lm, Um, p = F.L, F.U, F.p
+    assert sorted(p.tolist()) == list(range(1, n + 1))
+    assert np.allclose(A[p - 1, :], Lm @ Um, rtol=1e-12, atol=1e-12)
+    assert np.array_equal(np.diag(Lm), np.ones(n)) and np.array_equal(Lm, np.tril(Lm))
+    assert np.array_equal(Um, np.triu(Um)) and np.array_equal(Um, np.tril(Um, l + u))
+    assert F.issuccess() and F.size() == (n, n)
