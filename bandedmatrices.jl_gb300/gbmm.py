@@ -20,9 +20,10 @@ def _bnds(m: int, n: int) -> tuple[int, int]:
     return (m - 1, n - 1)
 
 
-def prodbandwidths(A: BandedMatrix, B: BandedMatrix) -> tuple[int, int]:
-    """prodbandwidths (src/generic/utils.jl:19-21)."""
-    return (A.l + B.l, A.u + B.u)
+def prodbandwidths(*As: BandedMatrix) -> tuple[int, int]:
+    """prodbandwidths (src/generic/utils.jl:19-21): the bandwidths of the product A1*A2*...,
+    the sums of the factors' bandwidths; (0, 0) for no factor."""
+    return (sum(A.l for A in As), sum(A.u for A in As))
 
 
 def _scale_band_rows(C: BandedMatrix, r0: int, r1: int, beta: float) -> None:

@@ -163,3 +163,19 @@ def test_banded_lu_views(bm, orc, n, l, u):
     assert np.array_equal(np.diag(Lm), np.ones(n)) and np.array_equal(Lm, np.tril(Lm))
     assert np.array_equal(Um, np.triu(Um)) and np.array_equal(Um, np.tril(Um, l + u))
     assert F.issuccess() and F.size() == (n, n)
+
+
+def test_product_bandwidths(bm):
+    """prodbandwidths (src/generic/utils.jl:19-21): sums of the factors' bandwidths, (0, 0)
+    for no factor, a single factor's own bandwidths; negative bandwidths add too."""
+    from importlib import import_module
+
+    gbmm = import_module(bm.__name__ + ".gbmm")
+    A = bm.BandedMatrix.zeros((6, 6), (2, 1), torch.float64, "cpu")
+    B = bm.BandedMatrix.zeros((6, 6), (0, 3), torch.float64, "cpu")
+    C = bm.BandedMatrix(torch.zeros(0, 6, dtype=torch.float64), 6, -1, -1)
+    assert gbmm.prodbandwidths() == (0, 0)
+    assert gbmm.prodbandwidths(A) == (2, 1)
+    assert gbmm.prodbandwidths(A, B) == (2, 4)
+    assert gbmm.prodbandwidths(A, B, A) == (4, 5)
+    assert gbmm.prodbandwidths(A, C) == (1, 0)
