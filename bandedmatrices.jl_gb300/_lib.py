@@ -32,6 +32,7 @@ SIGNATURES: dict[str, list] = {
     "bm_device_status": [P, I, P],
     "bm_launch_count": [],
     "bm_probe_fma_rate": [I, P, P],
+    "bm_wait_selftest": [i64, P, P],
     "bm_dgbmv": [C, i64, i64, i64, i64, D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmv": [C, i64, i64, i64, i64, F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm": [i64] * 9 + [D, P, i64, P, i64, D, P, i64, P],

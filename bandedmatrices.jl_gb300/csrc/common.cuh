@@ -93,9 +93,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Bounded wait for phase `phase` of `bar`.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-  for (uint32_t it = 0; it < kSpinLimit; ++it)
+// Bounded wait for phase `phase` of `bar`: at most `limit` polls (never more than
+// kSpinLimit).  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = kSpinLimit) {
+  if (limit > kSpinLimit) limit = kSpinLimit;
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, phase)) return true;
   return false;
 }

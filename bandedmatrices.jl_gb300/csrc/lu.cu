@@ -309,12 +309,15 @@ __device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i
 // over `order`) and solves it as one group.  Part 2: once the queue reaches
 // order[n_wide], each warp takes narrow systems on its own, in a shared-memory slice
 // of narrow_elems elements.  Every system is factored in place and its right-hand
-// sides solved; info[s] receives its gbtrf info.
+// sides solved; info[s] receives its gbtrf info.  A descriptor that is illegal, or
+// whose band exceeds the bounds its part's shared memory was sized for (wkl/wku,
+// nkl/nku), gets info[s] = -(field number) and is skipped; an order entry outside
+// [0, count) is skipped.
 template <typename T, int W>
 __global__ void __launch_bounds__(32 * W) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
                                                              const int32_t* __restrict__ order, i64 n_wide, T* AB,
                                                              i64* ipiv, T* B, i64* info, int32_t* counter,
-                                                             i64 narrow_elems) {
+                                                             i64 narrow_elems, i64 wkl, i64 wku, i64 nkl, i64 nku) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* base = reinterpret_cast<T*>(smem_raw);
   int idx;
@@ -322,6 +325,12 @@ __global__ void __launch_bounds__(32 * W) gbsv_batched_kernel(i64 count, const b
     idx = next_item<W>(counter, reinterpret_cast<int*>(base));
     if (idx >= n_wide) break;
     const int s = order ? order[idx] : idx;
+    if (s < 0 || s >= count) continue;
+    const i64 bad = desc_check(descs[s], wkl, wku);
+    if (bad) {
+      if (threadIdx.x == 0) info[s] = bad;
+      continue;
+    }
     gbsv_system<T, W>(descs[s], s, AB, ipiv, B, info, base);
     __syncthreads();
   }
@@ -336,8 +345,14 @@ __global__ void __launch_bounds__(32 * W) gbsv_batched_kernel(i64 count, const b
     }
     if (my >= count) break;
     const int s = order ? order[my] : my;
-    gbsv_system<T, 1>(descs[s], s, AB, ipiv, B, info, ws);
     my = -1;
+    if (s < 0 || s >= count) continue;
+    const i64 bad = desc_check(descs[s], nkl, nku);
+    if (bad) {
+      if (lane == 0) info[s] = bad;
+      continue;
+    }
+    gbsv_system<T, 1>(descs[s], s, AB, ipiv, B, info, ws);
   }
 }
 
@@ -464,8 +479,9 @@ static int gbsv_batched_launch(i64 count, const bm_gb_desc* descs, const int32_t
   const i64 grid = std::min<i64>((i64)num_sms() * per_sm, std::max<i64>(need, 1));
   r = cuda_status(cudaMemsetAsync(counter, 0, sizeof(int32_t), stream), name);
   if (r) return r;
-  gbsv_batched_kernel<T, W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(count, descs, order, sc.n_wide, AB, ipiv,
-                                                                           B, info, counter, ne);
+  gbsv_batched_kernel<T, W><<<(unsigned)grid, 32 * W, (int)bytes, stream>>>(
+      count, descs, order, sc.n_wide, AB, ipiv, B, info, counter, ne, sc.wide_kl, sc.wide_ku, sc.narrow_kl,
+      sc.narrow_ku);
   return launch_status(name);
 }
 

@@ -57,6 +57,24 @@ __device__ __forceinline__ int next_item(int32_t* counter, int* hdr) {
   return idx;
 }
 
+// Legality of one batch descriptor for a group whose shared memory was sized for
+// bandwidths up to (bound_kl, bound_ku): 0, or -(field number) of the first illegal
+// field (n 1, kl 2, ku 3, nrhs 4, ab_offset 5, ldab 6, b_offset 7, ldb 8,
+// ipiv_offset 9), which the batched kernels store as the system's info and skip the
+// system.  A band wider than the bound would run past the group's shared memory.
+__device__ __forceinline__ i64 desc_check(const bm_gb_desc& d, i64 bound_kl, i64 bound_ku) {
+  if (d.n < 0 || d.n > 0x7fffffffLL) return -1;
+  if (d.kl < 0 || d.kl > bound_kl) return -2;
+  if (d.ku < 0 || d.ku > bound_ku) return -3;
+  if (d.nrhs < 0 || d.nrhs > 0x7fffffffLL) return -4;
+  if (d.ab_offset < 0) return -5;
+  if (d.ldab < 2 * d.kl + d.ku + 1) return -6;
+  if (d.b_offset < 0) return -7;
+  if (d.ldb < (d.n > 1 ? d.n : 1)) return -8;
+  if (d.ipiv_offset < 0) return -9;
+  return 0;
+}
+
 // Group-wide maximum (NaN propagates); scratch: G doubles of shared memory.
 template <int G>
 __device__ __forceinline__ double grp_max(double v, double* scratch) {

@@ -50,7 +50,20 @@ struct MixedParams {
   double tol;
   int maxit;
   i64 group_elems;   // shared-memory floats per warp (narrow factor part, correct)
+  i64 wide_kl, wide_ku, narrow_kl, narrow_ku;  // band bounds the factor launch's shared memory was sized for
 };
+
+// A system whose descriptor is illegal or exceeds the launch's band bounds: info gets
+// -(field number), and the system takes no factorization and no refinement.
+__device__ __forceinline__ bool mixed_reject(const MixedParams& p, int s, i64 bkl, i64 bku, bool leader) {
+  const i64 bad = desc_check(p.descs[s], bkl, bku);
+  if (bad && leader) {
+    p.info[s] = bad;
+    p.iters[s] = -1;
+    p.berr[s] = 0.0;
+  }
+  return bad != 0;
+}
 
 // ------------------------------------------------------------------ factor
 template <int G>
@@ -119,7 +132,9 @@ __global__ void __launch_bounds__(32 * W) mixed_factor_kernel(const MixedParams 
   for (;;) {
     idx = next_item<W>(p.counter, reinterpret_cast<int*>(base));
     if (idx >= n_wide) break;
-    mixed_factor_system<W>(p, p.order ? p.order[idx] : idx, base);
+    const int s = p.order ? p.order[idx] : idx;
+    if (s < 0 || s >= p.count || mixed_reject(p, s, p.wide_kl, p.wide_ku, threadIdx.x == 0)) continue;
+    mixed_factor_system<W>(p, s, base);
     __syncthreads();
   }
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -132,8 +147,10 @@ __global__ void __launch_bounds__(32 * W) mixed_factor_kernel(const MixedParams 
       my = __shfl_sync(0xffffffffu, v, 0);
     }
     if (my >= p.count) break;
-    mixed_factor_system<1>(p, p.order ? p.order[my] : my, ws);
+    const int s = p.order ? p.order[my] : my;
     my = -1;
+    if (s < 0 || s >= p.count || mixed_reject(p, s, p.narrow_kl, p.narrow_ku, lane == 0)) continue;
+    mixed_factor_system<1>(p, s, ws);
   }
 }
 
@@ -322,6 +339,7 @@ __global__ void __launch_bounds__(32 * kResW, 1) mixed_residual_kernel(const Mix
     __syncthreads();
     if (idx >= p.count) break;
     const int s = p.order ? p.order[idx] : idx;
+    if (s < 0 || s >= p.count) continue;
     const int it = p.iters[s];
     if (it < 0) continue;  // converged, or no FP32 factor
     const bm_gb_desc d = p.descs[s];
@@ -365,7 +383,7 @@ __global__ void __launch_bounds__(32 * W) mixed_correct_kernel(const MixedParams
     v = __shfl_sync(0xffffffffu, v, 0);
     if (v >= p.count) break;
     const int s = p.order ? p.order[v] : v;
-    if (p.iters[s] < 0) continue;
+    if (s < 0 || s >= p.count || p.iters[s] < 0) continue;
     const bm_gb_desc d = p.descs[s];
     const int kl = (int)d.kl, ku = (int)d.ku, nr = (int)d.nrhs;
     const i64 n = d.n;
@@ -406,6 +424,7 @@ __global__ void __launch_bounds__(kBlkThreads, 4) mixed_lu_blocked_kernel(const 
     __syncthreads();
     if (idx >= p.count) break;
     const int s = p.order ? p.order[idx] : idx;
+    if (s < 0 || s >= p.count || mixed_reject(p, s, p.wide_kl, p.wide_ku, threadIdx.x == 0)) continue;
     const bm_gb_desc d = p.descs[s];
     const i64 inf = blk_lu_cta(d.n, (int)d.kl, (int)d.ku, p.AB + d.ab_offset, d.ldab, p.AB32 + d.ab_offset, d.ldab,
                                p.ipiv + d.ipiv_offset, smem_raw, stage != 0);
@@ -435,7 +454,7 @@ __global__ void __launch_bounds__(32 * W, 16 / W) mixed_solve_blocked_kernel(con
     if (v >= 2 * p.count) break;
     const bool tail = v >= p.count;
     const int s = p.order ? p.order[tail ? v - p.count : v] : (tail ? v - (int)p.count : v);
-    if (p.iters[s] < 0) continue;
+    if (s < 0 || s >= p.count || p.iters[s] < 0) continue;
     const bm_gb_desc d = p.descs[s];
     const i64 n = d.n, nrhs = d.nrhs;
     if (tail && nrhs <= kSolveNR) continue;
@@ -606,11 +625,19 @@ static int dsgbsv_batched_impl(const MixedParams& p, const bm_gb_schedule* sc, c
   if (p.count == 0) return BM_OK;
   const i64 kl_all = std::max(sc->n_wide > 0 ? sc->wide_kl : 0, sc->n_wide < p.count ? sc->narrow_kl : 0);
   const i64 ku_all = std::max(sc->n_wide > 0 ? sc->wide_ku : 0, sc->n_wide < p.count ? sc->narrow_ku : 0);
+  MixedParams q = p;
   if (blk_lu_fits(kl_all, ku_all) && blk_solve_fits(kl_all, ku_all) &&
-      blk_smem_bytes(kl_all, ku_all, false) <= 227 * 1024)
-    return mixed_launch_blocked(p, kl_all, ku_all, stream, name);
-  if (sc->warps == 8) return mixed_launch<8>(p, *sc, stream, name);
-  return mixed_launch<4>(p, *sc, stream, name);
+      blk_smem_bytes(kl_all, ku_all, false) <= 227 * 1024) {
+    q.wide_kl = q.narrow_kl = kl_all;  // one CTA per system, sized for the widest band
+    q.wide_ku = q.narrow_ku = ku_all;
+    return mixed_launch_blocked(q, kl_all, ku_all, stream, name);
+  }
+  q.wide_kl = sc->wide_kl;
+  q.wide_ku = sc->wide_ku;
+  q.narrow_kl = sc->narrow_kl;
+  q.narrow_ku = sc->narrow_ku;
+  if (sc->warps == 8) return mixed_launch<8>(q, *sc, stream, name);
+  return mixed_launch<4>(q, *sc, stream, name);
 }
 
 }  // namespace bm

@@ -94,5 +94,34 @@ extern "C" int bm_device_status(int* status_out, int clear, bm_stream_t stream) 
   return bm::cuda_status(cudaStreamSynchronize(s), "bm_device_status");
 }
 
+// Bounded-wait self-test: one thread waits, through the same mbar_wait the streaming
+// kernels use, for a phase of an mbarrier that nothing arrives at.  The wait gives up
+// after `limit` polls, the kernel records BM_STATUS_TIMEOUT in the status word and
+// returns, and the context stays usable.  `done` (device int) is set to 1 when the
+// kernel has returned from its wait.
+namespace bm {
+__global__ void wait_selftest_kernel(uint32_t limit, int* status, int* done) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    if (!mbar_wait(&bar, 0u, limit)) record_status(status, BM_STATUS_TIMEOUT);
+    *done = 1;
+  }
+}
+}  // namespace bm
+
+extern "C" int bm_wait_selftest(int64_t spin_limit, int* done, bm_stream_t stream) {
+  if (spin_limit < 1 || spin_limit > (int64_t)bm::kSpinLimit) return -1;
+  if (!done) return -2;
+  int* w = bm::status_word();
+  if (!w) {
+    bm::set_error("bm_wait_selftest: status word unavailable");
+    return BM_ERR_CUDA;
+  }
+  bm::wait_selftest_kernel<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>((uint32_t)spin_limit, w, done);
+  return bm::launch_status("bm_wait_selftest");
+}
+
 // Kernels this library has enqueued in the process (captured launches included).
 extern "C" unsigned long long bm_launch_count(void) { return bm::g_launches.load(std::memory_order_relaxed); }

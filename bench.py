@@ -74,78 +74,138 @@ def _openblas():
     return L
 
 
-def cpu_sweep(steps: int, warmup: int, n_cpu: int = 1 << 21):
-    """Time OpenBLAS gbmv (all host threads) and the _gbmm! column loop on a bounded sample:
-    the same bandwidths and dtypes at n = 2^21 (gbmv) and the full n = 2^20 (gbmm)."""
+def _fill(a, kind: str, seed: int, threads: int = 16) -> None:
+    """Fill a contiguous numpy array in place with uniform(-1,1) ('u') or standard normal
+    ('n') values, in parallel chunks, each with its own seeded PCG64 stream (numpy's
+    generators release the GIL while they fill)."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    flat = a.reshape(-1, order="F" if a.flags.f_contiguous else "C")
+    chunks = np.array_split(np.arange(flat.size), threads)
+
+    def work(i):
+        if not len(chunks[i]):
+            return
+        v = flat[chunks[i][0]: chunks[i][-1] + 1]
+        rng = np.random.default_rng([seed, i])
+        if kind == "u":
+            rng.random(out=v, dtype=v.dtype)
+            v *= 2
+            v -= 1
+        else:
+            rng.standard_normal(out=v, dtype=v.dtype)
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(work, range(threads)))
+
+
+def cpu_operands():
+    """Host operands of the sweep at the full sizes: the six gbmv cases at n = 2^24 and
+    the two banded_mul cases at n = 2^20 (uniform(-1,1) bands, randn x)."""
+    import numpy as np
+
+    gbmv = []
+    for k, (dt, lu) in enumerate(GBMV_CASES):
+        nt = np.float32 if dt == "f32" else np.float64
+        A = np.empty((2 * lu + 1, N_GBMV), dtype=nt, order="F")
+        _fill(A, "u", 100 + k)
+        x = np.empty(N_GBMV, dtype=nt)
+        _fill(x, "n", 200 + k)
+        gbmv.append((dt, lu, A, x, np.zeros(N_GBMV, dtype=nt)))
+    mm = []
+    for k, dt in enumerate(("f32", "f64")):
+        nt = np.float32 if dt == "f32" else np.float64
+        A = np.empty((2 * LU_GBMM + 1, N_GBMM), dtype=nt, order="F")
+        B = np.empty((2 * LU_GBMM + 1, N_GBMM), dtype=nt, order="F")
+        _fill(A, "u", 300 + k)
+        _fill(B, "u", 400 + k)
+        mm.append((dt, A, B, np.zeros((4 * LU_GBMM + 1, N_GBMM), dtype=nt, order="F")))
+    return gbmv, mm
+
+
+def cpu_sweep(steps: int, warmup: int, one_thread_steps: int = 3):
+    """The reference's CPU path for the sweep, on the host cores, at the full sizes:
+    OpenBLAS {s,d}gbmv (the routine BandedMatrices.jl ccalls for A*x) for the six
+    n = 2^24 cases, and the _gbmm! column loop (gbmm.jl:296-340, restated in C over the
+    same OpenBLAS gbmv) for the two n = 2^20 products.  `warmup` untimed steps, then
+    `steps` timed ones with all OpenBLAS threads; value = bytes of a step / median step
+    time.  Then `one_thread_steps` steps with OpenBLAS on one thread, reported beside."""
     import numpy as np
 
     L = _openblas()
     threads = int(L.scipy_openblas_get_num_threads())
-    rng = np.random.default_rng(0)
-    cases = []
-    for dt, lu in GBMV_CASES:
-        nt = np.float32 if dt == "f32" else np.float64
-        A = np.asfortranarray(rng.uniform(-1, 1, (2 * lu + 1, n_cpu)).astype(nt))
-        x = rng.standard_normal(n_cpu).astype(nt)
-        y = np.zeros(n_cpu, dtype=nt)
-        fn = L.scipy_cblas_sgbmv if dt == "f32" else L.scipy_cblas_dgbmv
-        args = (102, 111, n_cpu, n_cpu, lu, lu, 1.0, A.ctypes.data, 2 * lu + 1, x.ctypes.data, 1, 0.0, y.ctypes.data, 1)
-        cases.append((fn, args, gbmv_bytes(n_cpu, lu, lu, nt().itemsize), (A, x, y)))  # keep buffers alive
-    # _gbmm!: one gbmv per column of C (gbmm.jl:296-340), at the full n = 2^20
-    n_mm = 1 << 20
-    mm = []
-    for dt in ("f32", "f64"):
-        nt = np.float32 if dt == "f32" else np.float64
-        A = np.asfortranarray(rng.uniform(-1, 1, (33, n_mm)).astype(nt))
-        B = np.asfortranarray(rng.uniform(-1, 1, (33, n_mm)).astype(nt))
-        C = np.zeros((65, n_mm), dtype=nt, order="F")
-        mm.append((dt, A, B, C, nt().itemsize))
+    gbmv, mm = cpu_operands()
 
     import oracle  # CPU-baseline leg: the _gbmm! column loop restated in C over OpenBLAS gbmv
 
     orl = oracle.lib()
     fptr = {"f32": ctypes.cast(L.scipy_cblas_sgbmv, ctypes.c_void_p).value,
             "f64": ctypes.cast(L.scipy_cblas_dgbmv, ctypes.c_void_p).value}
-
-    def gbmm_cpu(dt, A, B, C, s):
-        fn = orl.or_sgbmm_percol_cblas if dt == "f32" else orl.or_dgbmm_percol_cblas
-        T = ctypes.c_float if dt == "f32" else ctypes.c_double
-        fn(ctypes.c_void_p(fptr[dt]), n_mm, n_mm, n_mm, LU_GBMM, LU_GBMM, LU_GBMM, LU_GBMM, T(1.0),
-           ctypes.c_void_p(A.ctypes.data), 33, ctypes.c_void_p(B.ctypes.data), 33, T(0.0),
-           ctypes.c_void_p(C.ctypes.data), 65)
+    step_bytes = (sum(gbmv_bytes(N_GBMV, lu, lu, A.itemsize) for _, lu, A, _, _ in gbmv)
+                  + sum(gbmm_bytes(N_GBMM, LU_GBMM, LU_GBMM, A.itemsize) for _, A, _, _ in mm))
 
     def one_step():
-        t_gbmv = 0.0
-        bytes_gbmv = 0
-        for fn, args, nb, _keep in cases:
-            t0 = time.perf_counter()
-            fn(*args)
-            t_gbmv += time.perf_counter() - t0
-            bytes_gbmv += nb
-        t_mm = 0.0
-        bytes_mm = 0
-        for dt, A, B, C, s in mm:
-            t0 = time.perf_counter()
-            gbmm_cpu(dt, A, B, C, s)
-            t_mm += time.perf_counter() - t0
-            bytes_mm += gbmm_bytes(n_mm, LU_GBMM, LU_GBMM, s)
-        return t_gbmv, bytes_gbmv, t_mm, bytes_mm
+        t0 = time.perf_counter()
+        for dt, lu, A, x, y in gbmv:
+            fn = L.scipy_cblas_sgbmv if dt == "f32" else L.scipy_cblas_dgbmv
+            fn(102, 111, N_GBMV, N_GBMV, lu, lu, 1.0, A.ctypes.data, 2 * lu + 1, x.ctypes.data, 1, 0.0,
+               y.ctypes.data, 1)
+        t1 = time.perf_counter()
+        for dt, A, B, C in mm:
+            fn = orl.or_sgbmm_percol_cblas if dt == "f32" else orl.or_dgbmm_percol_cblas
+            T = ctypes.c_float if dt == "f32" else ctypes.c_double
+            w = 2 * LU_GBMM + 1
+            fn(ctypes.c_void_p(fptr[dt]), N_GBMM, N_GBMM, N_GBMM, LU_GBMM, LU_GBMM, LU_GBMM, LU_GBMM, T(1.0),
+               ctypes.c_void_p(A.ctypes.data), w, ctypes.c_void_p(B.ctypes.data), w, T(0.0),
+               ctypes.c_void_p(C.ctypes.data), 2 * w - 1)
+        t2 = time.perf_counter()
+        return t1 - t0, t2 - t1
 
-    for _ in range(warmup):
-        one_step()
-    samples = [one_step() for _ in range(max(1, steps))]
-    t = sum(s[0] + s[2] for s in samples)
-    by = sum(s[1] + s[3] for s in samples)
-    return {
-        "value": by / t / 1e9,
-        "gbmv_GBps": sum(s[1] for s in samples) / sum(s[0] for s in samples) / 1e9,
-        "gbmm_GBps": sum(s[3] for s in samples) / sum(s[2] for s in samples) / 1e9,
-        "sec_per_step": t / len(samples),
+    def run(k, w):
+        for _ in range(w):
+            one_step()
+        return [one_step() for _ in range(max(1, k))]
+
+    s_all = run(steps, warmup)
+    s_one = []
+    if one_thread_steps > 0 and hasattr(L, "scipy_openblas_set_num_threads"):
+        L.scipy_openblas_set_num_threads(1)
+        try:
+            s_one = run(one_thread_steps, 0)
+        finally:
+            L.scipy_openblas_set_num_threads(threads)
+    gb_bytes = step_bytes - sum(gbmm_bytes(N_GBMM, LU_GBMM, LU_GBMM, A.itemsize) for _, A, _, _ in mm)
+    med = statistics.median(a + b for a, b in s_all)
+    out = {
+        "value": step_bytes / med / 1e9,
+        "sec_per_step": med,
+        "sec_total": sum(a + b for a, b in s_all),
+        "steps": len(s_all),
+        "warmup": warmup,
+        "gbmv_GBps": gb_bytes / statistics.median(a for a, _ in s_all) / 1e9,
+        "gbmm_GBps": (step_bytes - gb_bytes) / statistics.median(b for _, b in s_all) / 1e9,
         "threads": threads,
-        "sample": (f"OpenBLAS {{s,d}}gbmv via SciPy's bundled libscipy_openblas (the BLAS routine "
-                   f"BandedMatrices.jl ccalls; Julia absent), {threads} threads, same l,u,dtypes at n=2^21; "
-                   f"_gbmm! column loop (restated in C) over the same OpenBLAS gbmv at n=2^20"),
+        "host_cores": os.cpu_count(),
+        "sample": (f"the full sweep (gbmv n=2^24 l=u in {{1,8,32}} f32+f64; banded_mul n=2^20 l=u=16 f32+f64) on "
+                   f"the host: OpenBLAS {{s,d}}gbmv via SciPy's bundled libscipy_openblas (the BLAS routine "
+                   f"BandedMatrices.jl ccalls; Julia absent) and the _gbmm! column loop restated in C over it; "
+                   f"median of {len(s_all)} steps after {warmup} warm-up, {threads} threads"),
     }
+    if s_one:
+        out["one_thread"] = {"value": step_bytes / statistics.median(a + b for a, b in s_one) / 1e9,
+                             "steps": len(s_one),
+                             "gbmv_GBps": gb_bytes / statistics.median(a for a, _ in s_one) / 1e9,
+                             "gbmm_GBps": (step_bytes - gb_bytes) / statistics.median(b for _, b in s_one) / 1e9}
+    del np
+    return out
+
+
+def bench_config(world: int) -> dict:
+    """The `config` object of both arms' JSON lines (identical, so the lines compare)."""
+    return {"workload": WORKLOAD, "l2": "every operand set > 129 MB L2 (no flush needed)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
 # --------------------------------------------------------------------------- clocks
@@ -389,15 +449,14 @@ def run_gpu(args, rank, world):
     # e2e through the public API with host buffers
     e2e = None
     if rank == 0 or world > 1:
-        e2e = run_e2e(bm, gb, mm, dev, stream, max(1, min(args.steps, 3)))
+        e2e = run_e2e(bm, gb, mm, dev, stream, args.steps)
     out = None
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (torch Philox, seeded)",
-            "config": {"workload": WORKLOAD, "l2": "every operand set > 129 MB L2 (no flush needed)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": bench_config(world),
             "roofline": {"bound": "hbm", "kernel": dom["case"], "achieved": dom["GBps"], "peak": peak,
                          "unit": "GB/s", "frac": dom["GBps"] / peak, "traffic": traffic,
                          "peak_source": f"{peak_kind} hbm_gbs",
@@ -806,14 +865,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_sweep(max(1, min(args.steps, 3)), min(args.warmup, 1))
+        cb = cpu_sweep(args.steps, args.warmup)
+        cpu = {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
+               "sample": cb["sample"], "host_cores": cb["host_cores"], "gbmv_GBps": cb["gbmv_GBps"],
+               "gbmm_GBps": cb["gbmm_GBps"], "one_thread": cb.get("one_thread")}
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["sec_per_step"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic (numpy PCG64)", "config": {"workload": WORKLOAD},
-            "cpu_baseline": {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
-                             "sample": cb["sample"], "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"]},
+            "steps": cb["steps"], "warmup": cb["warmup"], "ms_per_step": cb["sec_per_step"] * 1e3,
+            "timed_s": cb["sec_total"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic (numpy PCG64, seeded)", "config": bench_config(args.gpus),
+            "cpu_baseline": cpu,
             "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
         return
@@ -841,9 +902,11 @@ def main():
         if not args.no_cpu_baseline:
             if not args.sweep_only:
                 out["cpu_baseline_solvers"] = cpu_lu_baselines()
-            cb = cpu_sweep(1, 1)
+            cb = cpu_sweep(5, 1, one_thread_steps=1)
             out["cpu_baseline"] = {"value": cb["value"], "unit": "GB/s", "cores": cb["threads"], "kind": "reference",
-                                   "sample": cb["sample"], "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"]}
+                                   "sample": cb["sample"], "host_cores": cb["host_cores"],
+                                   "gbmv_GBps": cb["gbmv_GBps"], "gbmm_GBps": cb["gbmm_GBps"],
+                                   "one_thread": cb.get("one_thread")}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

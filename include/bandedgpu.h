@@ -55,6 +55,14 @@ unsigned long long bm_launch_count(void);
  * FP64 pipe bounds.  Runs a short probe kernel; synchronises the stream. */
 int bm_probe_fma_rate(int elem_bytes, double *fma_per_s, bm_stream_t stream);
 
+/* Diagnostics (no reference counterpart).  Self-test of the bounded in-kernel waits:
+ * enqueues a one-thread kernel that waits, with the same helper the streaming kernels
+ * use, for an mbarrier phase that nothing completes, giving up after spin_limit polls
+ * (1 <= spin_limit <= 2^26).  On expiry the kernel sets bit 0 (timeout) of the device
+ * status word (read it with bm_device_status) and returns; *done (device int) is set
+ * to 1 once the wait has ended.  Nothing faults, traps or hangs. */
+int bm_wait_selftest(int64_t spin_limit, int *done, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ gbmv
  * y <- alpha*op(A)*x + beta*y, op = 'N' | 'T' (| 'C' = 'T' for real types).
  * Replaces the dgbmv_/sgbmv_ ccall of src/blas.jl:16-28 and the stdlib
@@ -173,7 +181,12 @@ typedef struct {
 /* Factor and solve every system of a batch in one persistent launch: warps take
  * systems from a device work queue in the order `order` (device int32 list of
  * system indices, most expensive first; NULL = natural order).  info[s] (device)
- * receives system s's gbtrf info; systems with info != 0 are not solved.
+ * receives system s's gbtrf info; systems with info != 0 are not solved.  The
+ * kernel checks every descriptor before it touches the system: an illegal field, or
+ * a kl/ku above the bounds shared memory was sized for (max_kl/max_ku, or the
+ * schedule's), gives info[s] = -(field number: n 1, kl 2, ku 3, nrhs 4, ab_offset 5,
+ * ldab 6, b_offset 7, ldb 8, ipiv_offset 9) and the system is skipped; order entries
+ * outside [0, count) are skipped.
  * `counter` is one device int32 of workspace (reset by the call).  max_kl/max_ku
  * bound the bandwidths in the batch (shared memory is sized from them).  No
  * allocation, no host synchronisation: the call can be captured in a CUDA graph.
@@ -213,7 +226,9 @@ int bm_sgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_t
  * ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol or maxit corrections.  X
  * receives the solutions (B's layout), iters/berr the corrections taken and the
  * final backward error per system (max over its right-hand sides), info the FP32
- * factorization's info.  R32 is FP32 workspace laid out like B but with leading
+ * factorization's info (or -(field number) for a descriptor the kernel rejects, as
+ * in bm_dgbsv_batched; such a system is neither factored nor refined).  R32 is FP32
+ * workspace laid out like B but with leading
  * dimension n (n*nrhs floats per system at its b_offset); counter is 4 int32 of
  * workspace.  kl + ku <= 256 per system; maxit is capped at 100.  The call enqueues
  * a factor launch, then maxit pairs of correction / FP64-residual launches (pairs

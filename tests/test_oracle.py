@@ -217,3 +217,36 @@ def test_adjoint_formula(orc):
         dm = data.copy(); dm[r, j] -= h
         fd = (loss(dp, b) - loss(dm, b)) / (2 * h)
         assert abs(fd - gband[r, j]) < 1e-6 * max(1.0, abs(fd))
+
+
+BLOCKED = os.path.join(os.path.dirname(__file__), "golden", "blocked_golden.npz")
+# normwise factor agreement with OpenBLAS's blocked dgbtrf (dgemm/dtrsm trailing
+# updates in another order than dgbtf2's), and solution agreement per case (set by
+# each case's conditioning; c5 is a diffusion operator, r512 unshifted random)
+BLOCKED_TOL = {"c4a": (1e-12, 1e-11), "c5": (1e-12, 1e-12), "r512": (1e-12, 1e-9)}
+
+
+@pytest.mark.parametrize("name", ["c4a", "c5", "r512"])
+def test_gbtf2_blocked_regime_golden(orc, name):
+    """The dgbtf2 restatement against OpenBLAS in its blocked regime (kl >= its block
+    size), at the bandwidths of the wide-band workloads: identical pivots, factors and
+    solutions within BLOCKED_TOL, backward error <= 1e-12."""
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_blocked_golden as mb
+
+    gb = np.load(BLOCKED)
+    data, l, u, b = mb.case_data(name, gb["c5_kfield"])
+    n = data.shape[1]
+    LU, ipiv, info = orc.gbtf2(n, n, l, u, orc.lu_storage(data, n, l, u))
+    assert info == 0
+    assert np.array_equal(ipiv, gb[f"{name}_pivoff"].astype(np.int64) + np.arange(1, n + 1))
+    cols = gb[f"{name}_cols"]
+    ftol, xtol = BLOCKED_TOL[name]
+    assert _rel(LU[:, cols], gb[f"{name}_LUcols"]) <= ftol
+    x = orc.gbtrs("N", n, l, u, LU, ipiv, b)
+    assert _rel(x, gb[f"{name}_x"]) <= xtol
+    r = orc.gbmv("N", n, n, l, u, 1.0, data, x) - b
+    rowsum = orc.gbmv("N", n, n, l, u, 1.0, np.abs(data), np.ones(n))
+    assert np.abs(r).max() / (rowsum.max() * np.abs(x).max() + np.abs(b).max()) <= 1e-12
