@@ -58,6 +58,8 @@ SIGNATURES: dict[str, list] = {
     "bm_dgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P],
     "bm_sgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P],
     "bm_dsgbsv_batched_sched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, P],
+    "bm_dsgbsv": [i64, i64, i64, i64, P, i64, P, i64, P, i64, P, P, P, D, i64, P, P, P, P],
+    "bm_sgbtrf_tc": [i64, i64, i64, P, i64, P, i64, P, P, P],
 }
 
 # bm_gb_desc as a numpy structured dtype (9 x int64, C layout)

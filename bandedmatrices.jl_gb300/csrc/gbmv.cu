@@ -38,6 +38,7 @@ struct GbmvParams {
   uint32_t stage_bytes;  // bytes per ring slot (A part + x part), multiple of 128
   uint32_t xoff;         // byte offset of the x part inside a slot
   int* status;
+  const int* skip;       // device flag: nonzero -> the launch does nothing (NULL: always run)
 };
 
 template <typename T>
@@ -132,6 +133,7 @@ __device__ __forceinline__ bool produce_tile(const GbmvParams<T>& p, unsigned ch
 
 template <typename T, bool TRANS>
 __global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams<T> p) {
+  if (p.skip && *reinterpret_cast<volatile const int*>(p.skip)) return;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* ready = full + 8;
@@ -293,7 +295,9 @@ __global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams
 // Any strides: one thread per output element, same accumulation order.
 template <typename T, bool TRANS>
 __global__ void gbmv_strided_kernel(i64 m, i64 n, i64 kl, i64 ku, T alpha, const T* __restrict__ A, i64 lda,
-                                    const T* __restrict__ x, i64 incx, T beta, T* __restrict__ y, i64 incy) {
+                                    const T* __restrict__ x, i64 incx, T beta, T* __restrict__ y, i64 incy,
+                                    const int* skip) {
+  if (skip && *reinterpret_cast<volatile const int*>(skip)) return;
   const i64 leny = TRANS ? n : m, lenx = TRANS ? m : n;
   const i64 kx = incx > 0 ? 0 : -(lenx - 1) * incx;
   const i64 ky = incy > 0 ? 0 : -(leny - 1) * incy;
@@ -317,9 +321,11 @@ __global__ void gbmv_strided_kernel(i64 m, i64 n, i64 kl, i64 ku, T alpha, const
   }
 }
 
+// skip: optional device flag read by the kernels at launch (nonzero: no work), so a
+// caller can enqueue the call ahead of a device-side decision.
 template <typename T>
 static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T* A, i64 lda, const T* x, i64 incx,
-                     T beta, T* y, i64 incy, cudaStream_t stream, const char* name) {
+                     T beta, T* y, i64 incy, cudaStream_t stream, const char* name, const int* skip = nullptr) {
   const bool notr = (trans == 'N' || trans == 'n');
   if (!notr && !(trans == 'T' || trans == 't' || trans == 'C' || trans == 'c')) return -1;
   if (m < 0) return -2;
@@ -377,10 +383,10 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
     const i64 blocks = std::min<i64>(ceil_div(leny, threads), (i64)nsm * 32);
     if (notr)
       gbmv_strided_kernel<T, false><<<(unsigned)blocks, threads, 0, stream>>>(m, n, kl, ku, alpha, A, lda, x, incx,
-                                                                              beta, y, incy);
+                                                                              beta, y, incy, skip);
     else
       gbmv_strided_kernel<T, true><<<(unsigned)blocks, threads, 0, stream>>>(m, n, kl, ku, alpha, A, lda, x, incx,
-                                                                             beta, y, incy);
+                                                                             beta, y, incy, skip);
     return launch_status(name);
   }
 
@@ -397,6 +403,7 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   p.xoff = (uint32_t)abytes;
   p.stage_bytes = (uint32_t)(abytes + xbytes);
   p.status = status_word();
+  p.skip = skip;
   const int smem = 256 + stages * (int)p.stage_bytes;
   if (smem > 227 * 1024) {
     set_error("%s: internal tile selection exceeded shared memory (%d bytes)", name, smem);
@@ -411,6 +418,12 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   else
     gbmv_tma_kernel<T, true><<<(unsigned)grid, kGbmvThreads, smem, stream>>>(p);
   return launch_status(name);
+}
+
+// Float64 gbmv with a skip flag, for the other translation units of the library.
+int dgbmv_flagged(char trans, i64 m, i64 n, i64 kl, i64 ku, double alpha, const double* A, i64 lda, const double* x,
+                  i64 incx, double beta, double* y, i64 incy, const int* skip, cudaStream_t stream, const char* name) {
+  return gbmv_impl<double>(trans, m, n, kl, ku, alpha, A, lda, x, incx, beta, y, incy, stream, name, skip);
 }
 
 }  // namespace bm

@@ -531,10 +531,9 @@ static int gbsv_batched_impl(i64 count, const bm_gb_desc* descs, const int32_t* 
 
 // ---------------------------------------------------------------------------
 // Allocation-free batched solve.  Some callers of this library cannot call
-// cudaMalloc at solve time: code running while a stream is being captured into a
-// CUDA graph, real-time loops that must not block on the allocator, and hosts whose
-// device memory is owned by another runtime's pool (Julia's CUDA.jl, PyTorch) and
-// that cannot hand the library a workspace.  For them, the scratch of the batched
+// cudaMalloc at solve time: real-time loops that must not block on the allocator,
+// and hosts whose device memory is owned by another runtime's pool (Julia's CUDA.jl,
+// PyTorch) and that cannot hand the library a workspace.  For them, the scratch of the batched
 // solve -- the work-queue counter and the longest-first processing order -- lives
 // in this file-scope device array instead of caller-provided memory.  Every GPU that
 // loads the library keeps these 256 KiB (plus 256 bytes) until the process exits.
@@ -572,7 +571,9 @@ __global__ void __launch_bounds__(1024) lpt_order_kernel(i64 count, const bm_gb_
   for (i64 s = threadIdx.x; s < count; s += blockDim.x) order[atomicAdd(&start[bin_of(s)], 1)] = (int32_t)s;
 }
 
-// Device address of g_noalloc_scratch on the current device, looked up once per device.
+// Device address of g_noalloc_scratch on the current device, looked up once per device
+// and cached for the life of the process (a cudaDeviceReset invalidates it: the
+// library must then be reloaded).
 static int noalloc_scratch(int32_t** out, const char* name) {
   static std::mutex mu;
   static int32_t* cache[64] = {nullptr};

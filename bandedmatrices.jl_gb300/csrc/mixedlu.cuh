@@ -63,7 +63,7 @@ __host__ __device__ inline i64 blk_smem_bytes(i64 kl, i64 ku, bool stage = true)
 // Factors system (n, kl, ku) from the FP64 band A (gbtrf storage: A(i,c) at row
 // kv + i - c, the matrix in rows kl..) into the FP32 storage A32 (same layout) and
 // ipiv (1-based).  Called by all kBlkThreads threads; returns info in every thread.
-__device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i64 ldab, float* __restrict__ A32,
+static __device__ i64 blk_lu_cta(i64 n, int kl, int ku, const double* __restrict__ A, i64 ldab, float* __restrict__ A32,
                           i64 ldab32, i64* __restrict__ ipiv, unsigned char* smem, bool stage) {
   constexpr int NB = kBlkNB, NT = kBlkThreads;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -396,12 +396,14 @@ constexpr int kSolveRingStride = 6 * 32;
 constexpr int kSolveRingFloats = (kSolveD + 1) * kSolveRingStride;
 
 // Forward sweep (dgbtrs 'N': interchange, then b(j+1:j+lm) -= b(j) L(j+1:j+lm, j)) for
-// nr <= kSolveNR right-hand sides B[:, 0..nr) (leading dim ldb); 32*NS >= kl+1+kSolveD.
-template <int NS>
+// nr <= NR right-hand sides B[:, 0..nr) (leading dim ldb); 32*NS >= kl+1+kSolveD.  The
+// ring holds kSolveD + 1 entries of STRIDE floats (STRIDE >= 32*NS).
+template <int NS, int NR = kSolveNR, int STRIDE = kSolveRingStride>
 __device__ __noinline__ void blk_fwd_warp(i64 n, int kl, int ku, int nr, const float* __restrict__ A32, i64 ldab,
                                           const i64* __restrict__ ipiv, float* __restrict__ B, i64 ldb,
                                           float* ring, int lane) {
-  constexpr int NR = kSolveNR, W = 32 * NS, D = kSolveD;
+  constexpr int W = 32 * NS, D = kSolveD;
+  static_assert(STRIDE >= 32 * NS, "ring entry too small");
   if (kl == 0 || n <= 1) return;
   const int kv = kl + ku;
   const i64 nst = n - 1;  // steps j = 0 .. n-2
@@ -420,7 +422,7 @@ __device__ __noinline__ void blk_fwd_warp(i64 n, int kl, int ku, int nr, const f
   // copies of step j's multipliers into ring entry e (rows held now)
   auto issue = [&](i64 j, int e) {
     const int lm = j < nst ? (int)min((i64)kl, n - 1 - j) : 0;
-    float* dst = ring + e * kSolveRingStride + lane;
+    float* dst = ring + e * STRIDE + lane;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       const i64 d = row[s] - j;
@@ -453,14 +455,14 @@ __device__ __noinline__ void blk_fwd_warp(i64 n, int kl, int ku, int nr, const f
     const int cn = (int)min((i64)32, nst - j0);
     for (int t = 0; t < cn; ++t) {
       const i64 j = j0 + t;
-      if (lane < 3 && j + kSolvePF < nst) {
+      if (lane < max(3, (kl + 31) / 32) && j + kSolvePF < nst) {
         const float* pf = A32 + (kv + 1) + (j + kSolvePF) * ldab + min(lane * 32, kl - 1);
         asm volatile("prefetch.global.L2 [%0];" ::"l"(pf));
       }
       cp_async_wait<D - 1>();
       float l[NS];
 #pragma unroll
-      for (int s = 0; s < NS; ++s) l[s] = ring[er * kSolveRingStride + 32 * s + lane];
+      for (int s = 0; s < NS; ++s) l[s] = ring[er * STRIDE + 32 * s + lane];
       issue(j + D, ew);
       er = er == D ? 0 : er + 1;
       ew = ew == D ? 0 : ew + 1;
@@ -499,11 +501,13 @@ __device__ __noinline__ void blk_fwd_warp(i64 n, int kl, int ku, int nr, const f
 }
 
 // Back substitution with U (bandwidth kv, dtbsv 'U','N'): x(j) = b(j) * (1/U(j,j)),
-// then b(j-kv .. j-1) -= x(j) U(:, j); 32*NS >= kv + 1 + kSolveD.
-template <int NS>
+// then b(j-kv .. j-1) -= x(j) U(:, j); 32*NS >= kv + 1 + kSolveD.  Ring entries of
+// STRIDE floats hold NS slots and, in the last 32 floats, the diagonal.
+template <int NS, int NR = kSolveNR, int STRIDE = kSolveRingStride>
 __device__ __noinline__ void blk_bwd_warp(i64 n, int kv, int nr, const float* __restrict__ A32, i64 ldab,
                                           float* __restrict__ B, i64 ldb, float* ring, int lane) {
-  constexpr int NR = kSolveNR, W = 32 * NS, D = kSolveD;
+  constexpr int W = 32 * NS, D = kSolveD, DG = STRIDE / 32 - 1;
+  static_assert(STRIDE >= 32 * (NS + 1), "ring entry too small");
   if (n <= 0) return;
   float b[NR][NS];
   i64 row[NS];
@@ -525,14 +529,14 @@ __device__ __noinline__ void blk_bwd_warp(i64 n, int kv, int nr, const float* __
     }
   }
   auto issue = [&](i64 j, int e) {  // step j's U column (and diagonal) into ring entry e
-    float* dst = ring + e * kSolveRingStride + lane;
+    float* dst = ring + e * STRIDE + lane;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       const i64 d = j - row[s];
       const bool ok = j >= 0 && d >= 1 && d <= kv && row[s] >= 0;
       cp_async_elem(dst + 32 * s, ok ? A32 + (kv - d) + j * ldab : A32, ok);
     }
-    cp_async_elem(dst + 32 * 5, j >= 0 ? A32 + kv + j * ldab : A32, j >= 0);
+    cp_async_elem(dst + 32 * DG, j >= 0 ? A32 + kv + j * ldab : A32, j >= 0);
     cp_async_commit();
   };
   for (int u = 0; u < D; ++u) issue(top - u, u);
@@ -557,16 +561,16 @@ __device__ __noinline__ void blk_bwd_warp(i64 n, int kv, int nr, const float* __
     const int cn = (int)min((i64)32, j0 + 1);
     for (int t = 0; t < cn; ++t) {
       const i64 j = j0 - t;
-      if (lane < 5 && j - kSolvePF >= 0) {
+      if (lane < max(5, (kv + 32) / 32) && j - kSolvePF >= 0) {
         const float* pf = A32 + (j - kSolvePF) * ldab + min(lane * 32, kv);
         asm volatile("prefetch.global.L2 [%0];" ::"l"(pf));
       }
       cp_async_wait<D - 1>();
       float uc[NS];
-      const float* src = ring + er * kSolveRingStride + lane;
+      const float* src = ring + er * STRIDE + lane;
 #pragma unroll
       for (int s = 0; s < NS; ++s) uc[s] = src[32 * s];
-      const float rcp = __frcp_rn(src[32 * 5]);
+      const float rcp = __frcp_rn(src[32 * DG]);
       issue(j - D, ew);
       er = er == D ? 0 : er + 1;
       ew = ew == D ? 0 : ew + 1;
@@ -591,7 +595,7 @@ __device__ __noinline__ void blk_bwd_warp(i64 n, int kv, int nr, const float* __
 
 // gbtrs 'N' with the FP32 factors for right-hand sides [c0, c0+nr) of B (nr <=
 // kSolveNR), by one warp; ring: kSolveRingFloats of this warp's shared memory.
-__device__ void blk_solve_warp(i64 n, int kl, int ku, int nr, const float* A32, i64 ldab, const i64* ipiv, float* B,
+static __device__ void blk_solve_warp(i64 n, int kl, int ku, int nr, const float* A32, i64 ldab, const i64* ipiv, float* B,
                                i64 ldb, float* ring, int lane) {
   const int kv = kl + ku;
   switch (blk_ns(kl)) {

@@ -1,9 +1,10 @@
 """Mixed-precision refined solve of one banded system (LAPACK DSGESV's scheme on a
-band): the Float64 band is rounded to Float32 and factored with partial pivoting
-(bm_sgbtrf); then x = LU32 \\ b and, until the backward error
-||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches ``tol``, the residual is
-formed in Float64 from the original band (bm_dgbmv) and the Float32 correction
-LU32 \\ r is added in Float64.  Every step runs on the device through the library.
+band), through bm_dsgbsv: the Float64 band is factored in Float32 with partial
+pivoting (for 64 <= l+u <= 256 by the tensor-core blocked LU), then x = LU32 \\ b and,
+until the backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) reaches
+``tol``, the residual is formed in Float64 from the original band and the Float32
+correction LU32 \\ r is added in Float64.  The whole loop is enqueued in one call and
+decided on the device: no host synchronisation until the caller reads the result.
 
 No counterpart in the reference; it replaces lu! + ldiv!
 (src/banded/BandedLU.jl:90-103, src/banded/linalg.jl:24-30) for callers that accept
@@ -11,48 +12,42 @@ a backward-error target, and is the single-system form of bm_dsgbsv_batched.
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
-from .banded import BandedMatrix, band_storage
-from .linalg import mul_
-from .lu import lu
+from . import _lib
+from .banded import BandedMatrix, _ptr, _require_cuda, _stream
 
 
-def solve_refined(A: BandedMatrix, b: torch.Tensor, tol: float = 1e-10, maxit: int = 50):
-    """x with ||b - A x||_inf <= tol (||A||_inf ||x||_inf + ||b||_inf), A square Float64.
+def solve_refined(A: BandedMatrix, b: torch.Tensor, tol: float = 1e-10, maxit: int = 30):
+    """x with ||b - A x||_inf <= tol (||A||_inf ||x||_inf + ||b||_inf), A square Float64
+    with bandwidths 0 <= l, u and l + u <= 256; b of length n, or n x nrhs.
 
-    Returns (x, stats) with stats = {"iters": corrections taken, "berr": final backward
-    error, "info": the Float32 factorization's info}; x is all NaN-free only when the
-    Float32 factorization succeeded (info == 0)."""
+    Returns (x, stats): stats = {"iters": corrections taken, "berr": final backward
+    error, "info": the Float32 factorization's info} as 0-d device tensors (reading
+    them synchronises); x is meaningful only when info == 0."""
     if A.dtype != torch.float64 or b.dtype != torch.float64:
         raise TypeError("solve_refined refines to Float64: A and b must be Float64")
-    n = A.shape[0]
-    d32 = band_storage(A.data.shape[0], n, torch.float32, A.device)
-    d32.copy_(A.data)
-    F = lu(BandedMatrix(d32, A.m, A.l, A.u))
-    cols = [b] if b.dim() == 1 else [b[:, c] for c in range(b.shape[1])]
-    absA = BandedMatrix(A.data.abs(), A.m, A.l, A.u)
-    ones = torch.ones(n, dtype=torch.float64, device=A.device)
-    rows = torch.empty(n, dtype=torch.float64, device=A.device)
-    mul_(rows, absA, ones)
-    anorm = float(rows.max()) if n else 0.0
-    xs, its, berr = [], 0, 0.0
-    for bc in cols:
-        bc = bc.contiguous()
-        x = F.solve(bc.float()).double()
-        bnorm = float(bc.abs().max()) if n else 0.0
-        r = torch.empty_like(bc)
-        it = 0
-        while True:
-            r.copy_(bc)
-            mul_(r, A, x, -1.0, 1.0)  # r = b - A x in Float64
-            den = anorm * float(x.abs().max()) + bnorm
-            be = float(r.abs().max()) / den if den > 0 else float(r.abs().max())
-            if not be > tol or it >= maxit:
-                break
-            x += F.solve(r.float()).double()
-            it += 1
-        xs.append(x)
-        its, berr = max(its, it), max(berr, be)
-    x = xs[0] if b.dim() == 1 else torch.stack(xs, dim=1)
-    return x, {"iters": its, "berr": berr, "info": F.info}
+    if A.m != A.n:
+        raise ValueError("solve_refined needs a square matrix")
+    if A.l < 0 or A.u < 0:
+        raise ValueError("solve_refined needs non-negative bandwidths")
+    _require_cuda(A.data, b)
+    n, kl, ku = A.n, A.l, A.u
+    B = b.reshape(n, -1) if b.dim() == 1 else b
+    nrhs = B.shape[1]
+    Bc = B.t().contiguous().t() if nrhs else B  # column-major, leading dim n
+    dev = A.device
+    X = torch.empty(nrhs, n, dtype=torch.float64, device=dev).t()
+    ipiv = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
+    swork = torch.empty((2 * kl + ku + 1) * n + n * nrhs + 1, dtype=torch.float32, device=dev)
+    work = torch.empty(n * nrhs + 3 * nrhs + 2, dtype=torch.float64, device=dev)
+    it = torch.empty(1, dtype=torch.int32, device=dev)
+    berr = torch.empty(1, dtype=torch.float64, device=dev)
+    info = torch.empty(1, dtype=torch.int64, device=dev)
+    _lib.call("bm_dsgbsv", n, kl, ku, nrhs, _ptr(A.data), A.lda, _ptr(Bc), max(1, n), _ptr(X), max(1, n), _ptr(ipiv),
+              _ptr(swork), _ptr(work), ctypes.c_double(tol), int(maxit), _ptr(it), _ptr(berr), _ptr(info),
+              _stream(dev))
+    x = X[:, 0] if b.dim() == 1 else X
+    return x, {"iters": it[0], "berr": berr[0], "info": info[0]}

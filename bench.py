@@ -677,7 +677,7 @@ def run_refined(bm, dev, stream):
     berr_plain = float(r.abs().max()) / (an * float(xp.abs().max()) + float(b.abs().max()))
     del A, b, x, xp, r
     return {"workload": "n=2^20, l=u=128, f64 randn + 16 I (kappa_1 ~ %.1e at n=2^16), b randn" % kappa,
-            "refined_ms": t_ref, "iters": st["iters"], "berr": st["berr"], "plain_fp64_ms": t_plain,
+            "refined_ms": t_ref, "iters": int(st["iters"]), "berr": float(st["berr"]), "plain_fp64_ms": t_plain,
             "berr_plain": berr_plain, "speedup_refined_vs_plain": t_plain / t_ref}
 
 

@@ -246,16 +246,49 @@ int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_
                             float *R32, int32_t *iters, double *berr, int32_t *counter, double tol, int64_t maxit,
                             bm_stream_t stream);
 
+/* Mixed-precision refined solve of ONE banded system (LAPACK DSGESV's scheme on band
+ * storage): the FP64 band AB ((kl+ku+1) x n, ldab >= kl+ku+1, A(i,c) at row ku+i-c, as
+ * BandedMatrix stores it; read only) is factored in FP32 with partial pivoting -- for
+ * 64 <= kl+ku <= 256 and kl <= 224 by the tensor-core blocked LU (trailing updates as
+ * kind::tf32 MMAs with hi/lo-split operands, FP32-level products), otherwise by the
+ * FP32 form of bm_sgbtrf -- and every right-hand side B (n x nrhs, ldb) is solved in
+ * FP32 and refined with FP64 residuals r = b - A x and FP64 updates until the
+ * backward error max_c ||r_c||_inf / (||A||_inf ||x_c||_inf + ||b_c||_inf) <= tol or
+ * maxit corrections (capped at 100).  X (n x nrhs, ldx) receives the solutions, ipiv
+ * the FP32 factorization's pivots, *info (device) its info (> 0: exactly singular in
+ * FP32; nothing is solved and *berr is +inf), *iter (device int32) the corrections
+ * taken, *berr (device double) the final backward error.  Workspace: swork, FP32,
+ * (2kl+ku+1)*n + n*nrhs floats (the factors in gbtrf layout, then the correction);
+ * work, FP64, n*nrhs + 3*nrhs + 2 doubles.  kl + ku <= 256.  The whole loop is
+ * enqueued at once and decided on the device (a flag turns the remaining launches
+ * into no-ops): no host synchronisation, no allocation.  No counterpart in the
+ * reference; it replaces lu! + ldiv! (src/banded/BandedLU.jl:90-103,
+ * src/banded/linalg.jl:24-30) for a caller that accepts a backward-error target. */
+int bm_dsgbsv(int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double *AB, int64_t ldab, const double *B,
+              int64_t ldb, double *X, int64_t ldx, int64_t *ipiv, float *swork, double *work, double tol,
+              int64_t maxit, int32_t *iter, double *berr, int64_t *info, bm_stream_t stream);
+
+/* The tensor-core FP32 factorization of bm_dsgbsv alone: AB as there, F the FP32 gbtrf
+ * storage ((2kl+ku+1) x n, ldf >= 2kl+ku+1) receiving L and U in the layout xGBTRS
+ * reads, ipiv n 1-based pivots, *info (device) LAPACK's info.  Needs 64 <= kl+ku <= 256
+ * and kl <= 224 (else BM_ERR_UNSUPPORTED).  The pivot is the largest |a| to 2^-15
+ * relative (the first row among near-equal magnitudes).  No counterpart in the
+ * reference (dgbtrf of lu!, src/banded/BandedLU.jl:98, in FP32 on tensor cores). */
+int bm_sgbtrf_tc(int64_t n, int64_t kl, int64_t ku, const double *AB, int64_t ldab, float *F, int64_t ldf,
+                 int64_t *ipiv, int64_t *info, bm_stream_t stream);
+
 /* Allocation-free variant of bm_dgbsv_batched, for callers that cannot allocate
- * device memory when they solve: code running under CUDA stream capture, real-time
- * loops that must not block on an allocator, and hosts whose device memory belongs
- * to another runtime's pool.  The caller passes only inputs and outputs; the work
- * queue and the longest-first order live in a 256 KiB static device array inside
- * the library, which every GPU that loads the library keeps until exit.  At most
- * 65536 systems per call (more: BM_ERR_UNSUPPORTED, see bm_last_error()).  The
- * first call on a device looks up the array's address and should come before any
- * stream capture.  All calls share the array, so calls that overlap on the GPU
- * (concurrent streams) race; serialise them.  No counterpart in the reference. */
+ * device memory when they solve: real-time loops that must not block on an
+ * allocator, and hosts whose device memory belongs to another runtime's pool (Julia's
+ * CUDA.jl, PyTorch) and that cannot hand the library a workspace.  The caller passes
+ * only inputs and outputs; the work queue and the longest-first order live in a
+ * 256 KiB static device array inside the library, which every GPU that loads the
+ * library keeps until exit.  At most 65536 systems per call (more:
+ * BM_ERR_UNSUPPORTED, see bm_last_error()).  The first call on a device looks up the
+ * array's address (once per device, cached for the process; after cudaDeviceReset
+ * reload the library) and should come before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (concurrent streams) race; serialise
+ * them.  No counterpart in the reference. */
 int bm_dgbsv_batched_noalloc(int64_t count, const bm_gb_desc *descs, double *AB, int64_t *ipiv, double *B,
                              int64_t *info, int64_t max_kl, int64_t max_ku, bm_stream_t stream);
 

@@ -110,7 +110,7 @@ def test_single_system_refined_wide_and_conditioned(bm, gpu, orc):
     A.data[ku] += 16.0
     b = torch.randn(n, dtype=torch.float64, device=gpu, generator=g)
     x, st = bm.solve_refined(A, b, tol=1e-10)
-    assert st["info"] == 0 and st["berr"] <= 1e-10 and st["iters"] >= 1
+    assert int(st["info"]) == 0 and float(st["berr"]) <= 1e-10 and int(st["iters"]) >= 1
     F = bm.lu(A)
     x64 = F.solve(b)
     kappa = float(A.data.abs().sum(0).max()) * F.inv_norm1_estimate()

@@ -1,7 +1,7 @@
 """The allocation-free batched solve (bm_dgbsv_batched_noalloc) against bm_dgbsv_batched.
 
-Callers that cannot allocate device memory at solve time (code under CUDA stream
-capture, real-time loops, hosts whose memory belongs to another runtime's pool) use the
+Callers that cannot allocate device memory at solve time (real-time loops that must not
+block on an allocator, hosts whose memory belongs to another runtime's pool) use the
 allocation-free entry point: it takes only inputs and outputs and keeps its scratch
 (work counter and longest-first order) in a static device array.  This checks, through
 the C ABI, that two calls in a row give exactly what the regular entry point gives, so
