@@ -18,6 +18,8 @@ from .batched import BandedBatch, lpt_order
 from .qr import BandedQR, lmul_, qr
 from .autograd import BandedSolve, banded_solve
 from .refine import solve_refined
+from .tri import (LowerTriangular, UnitLowerTriangular, UnitUpperTriangular, UpperTriangular, dense_gbmm_,
+                  gbmm_dense_)
 from . import pde, shard
 
 __all__ = [
@@ -25,7 +27,8 @@ __all__ = [
     "bandwidth", "bandwidths", "brand", "brandn", "gbmv", "ldiv", "mul", "mul_", "mul_t_", "load_library",
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
-    "solve_refined",
+    "solve_refined", "UpperTriangular", "LowerTriangular", "UnitUpperTriangular", "UnitLowerTriangular",
+    "gbmm_dense_", "dense_gbmm_",
     "BandedSolve", "banded_solve",
 ]
 

@@ -52,6 +52,12 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbqr_lmul": [C, i64, i64, i64, i64, P, i64, P, i64, i64, P, i64, P],
     "bm_dtbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
     "bm_stbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_dtbmv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_stbmv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_dgbmm_bd": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
+    "bm_sgbmm_bd": [i64] * 5 + [F, P, i64, P, i64, F, P, i64, P],
+    "bm_dgbmm_db": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
+    "bm_sgbmm_db": [i64] * 5 + [F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
     "bm_sgbsv_adjoint": [i64, i64, i64, i64, P, i64, P, P, P, P, P, P, i64, P, P],
     "bm_dsgbsv_batched": [i64, P, P, P, P, P, P, P, P, P, P, P, P, D, i64, i64, i64, P],

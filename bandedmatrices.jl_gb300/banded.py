@@ -186,6 +186,11 @@ class BandedMatrix:
         from . import linalg
         return linalg.mul(self, other)
 
+    def __rmatmul__(self, D):
+        """D * A for a dense D (src/generic/matmul.jl:258-271)."""
+        from .tri import _empty_colmajor, dense_gbmm_
+        return dense_gbmm_(_empty_colmajor(D.shape[0], self.n, D), D, self, 1.0, 0.0)
+
     def solve(self, b):
         """A \\ b (materialize!(::Ldiv), src/banded/linalg.jl:5-9)."""
         from . import linalg

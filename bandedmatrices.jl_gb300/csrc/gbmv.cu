@@ -420,6 +420,82 @@ static int gbmv_impl(char trans, i64 m, i64 n, i64 kl, i64 ku, T alpha, const T*
   return launch_status(name);
 }
 
+// Several gbmv products in one launch: vector v (blockIdx.y, grid-stride) computes
+// y_v = alpha op(A) x_v + beta y_v with x_v = x + v*xs (stride incx), y_v = y + v*ys
+// (stride incy), one thread per output in the order of gbmv_strided_kernel.  This is
+// banded x dense ('N', a column of B per vector) and dense x banded ('T', a row of D
+// per vector) -- the column / row loops of src/generic/matmul.jl:243-271.
+template <typename T, bool TRANS>
+__global__ void gbmv_multi_kernel(i64 m, i64 n, i64 kl, i64 ku, i64 nvec, T alpha, const T* __restrict__ A, i64 lda,
+                                  const T* __restrict__ x, i64 xs, i64 incx, T beta, T* __restrict__ y, i64 ys,
+                                  i64 incy) {
+  const i64 leny = TRANS ? n : m;
+  for (i64 v = blockIdx.y; v < nvec; v += gridDim.y) {
+    const T* xv = x + v * xs;
+    T* yv = y + v * ys;
+    for (i64 o = (i64)blockIdx.x * blockDim.x + threadIdx.x; o < leny; o += (i64)gridDim.x * blockDim.x) {
+      T* yp = yv + o * incy;
+      if (!TRANS) {
+        const i64 i = o;
+        const i64 jlo = max((i64)0, i - kl), jhi = min(n - 1, i + ku);
+        T acc = (beta == T(0)) ? T(0) : beta * *yp;
+        if (alpha != T(0))
+          for (i64 j = jlo; j <= jhi; ++j) acc = fma(alpha * xv[j * incx], A[j * lda + ku + i - j], acc);
+        *yp = acc;
+      } else {
+        const i64 j = o;
+        const i64 ilo = max((i64)0, j - ku), ihi = min(m - 1, j + kl);
+        T acc = T(0);
+        for (i64 i = ilo; i <= ihi; ++i) acc = fma(A[j * lda + ku + i - j], xv[i * incx], acc);
+        const T y0 = (beta == T(0)) ? T(0) : beta * *yp;
+        *yp = (alpha == T(0)) ? y0 : fma(alpha, acc, y0);
+      }
+    }
+  }
+}
+
+// C <- alpha A B + beta C: banded A (m x n), dense B (n x k, ldb), C (m x k, ldc).
+template <typename T>
+static int gbmm_bd_impl(i64 m, i64 n, i64 kl, i64 ku, i64 k, T alpha, const T* A, i64 lda, const T* B, i64 ldb,
+                        T beta, T* C, i64 ldc, cudaStream_t stream, const char* name) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (kl < 0) return -3;
+  if (ku < 0) return -4;
+  if (k < 0) return -5;
+  if (lda < kl + ku + 1) return -8;
+  if (ldb < std::max<i64>(1, n)) return -10;
+  if (ldc < std::max<i64>(1, m)) return -13;
+  if (m == 0 || k == 0 || (alpha == T(0) && beta == T(1))) return BM_OK;
+  const int threads = 256;
+  const i64 bx = std::min<i64>(ceil_div(m, threads), (i64)num_sms() * 8);
+  const i64 by = std::min<i64>(k, 65535);
+  gbmv_multi_kernel<T, false><<<dim3((unsigned)bx, (unsigned)by), threads, 0, stream>>>(
+      m, n, kl, ku, k, alpha, A, lda, B, ldb, 1, beta, C, ldc, 1);
+  return launch_status(name);
+}
+
+// C <- alpha D A + beta C: dense D (k x m, ldd), banded A (m x n), C (k x n, ldc).
+template <typename T>
+static int gbmm_db_impl(i64 m, i64 n, i64 kl, i64 ku, i64 k, T alpha, const T* D, i64 ldd, const T* A, i64 lda,
+                        T beta, T* C, i64 ldc, cudaStream_t stream, const char* name) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (kl < 0) return -3;
+  if (ku < 0) return -4;
+  if (k < 0) return -5;
+  if (ldd < std::max<i64>(1, k)) return -8;
+  if (lda < kl + ku + 1) return -10;
+  if (ldc < std::max<i64>(1, k)) return -13;
+  if (n == 0 || k == 0 || (alpha == T(0) && beta == T(1))) return BM_OK;
+  const int threads = 256;
+  const i64 bx = std::min<i64>(ceil_div(n, threads), (i64)num_sms() * 8);
+  const i64 by = std::min<i64>(k, 65535);
+  gbmv_multi_kernel<T, true><<<dim3((unsigned)bx, (unsigned)by), threads, 0, stream>>>(
+      m, n, kl, ku, k, alpha, A, lda, D, 1, ldd, beta, C, 1, ldc);
+  return launch_status(name);
+}
+
 // Float64 gbmv with a skip flag, for the other translation units of the library.
 int dgbmv_flagged(char trans, i64 m, i64 n, i64 kl, i64 ku, double alpha, const double* A, i64 lda, const double* x,
                   i64 incx, double beta, double* y, i64 incy, const int* skip, cudaStream_t stream, const char* name) {
@@ -440,4 +516,29 @@ extern "C" int bm_sgbmv(char trans, int64_t m, int64_t n, int64_t kl, int64_t ku
                         bm_stream_t stream) {
   return bm::gbmv_impl<float>(trans, m, n, kl, ku, alpha, A, lda, x, incx, beta, y, incy,
                               reinterpret_cast<cudaStream_t>(stream), "bm_sgbmv");
+}
+
+extern "C" int bm_dgbmm_bd(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, double alpha, const double* A,
+                           int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                           bm_stream_t stream) {
+  return bm::gbmm_bd_impl<double>(m, n, kl, ku, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                                  reinterpret_cast<cudaStream_t>(stream), "bm_dgbmm_bd");
+}
+extern "C" int bm_sgbmm_bd(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, float alpha, const float* A,
+                           int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                           bm_stream_t stream) {
+  return bm::gbmm_bd_impl<float>(m, n, kl, ku, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                                 reinterpret_cast<cudaStream_t>(stream), "bm_sgbmm_bd");
+}
+extern "C" int bm_dgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, double alpha, const double* D,
+                           int64_t ldd, const double* A, int64_t lda, double beta, double* C, int64_t ldc,
+                           bm_stream_t stream) {
+  return bm::gbmm_db_impl<double>(m, n, kl, ku, k, alpha, D, ldd, A, lda, beta, C, ldc,
+                                  reinterpret_cast<cudaStream_t>(stream), "bm_dgbmm_db");
+}
+extern "C" int bm_sgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, float alpha, const float* D,
+                           int64_t ldd, const float* A, int64_t lda, float beta, float* C, int64_t ldc,
+                           bm_stream_t stream) {
+  return bm::gbmm_db_impl<float>(m, n, kl, ku, k, alpha, D, ldd, A, lda, beta, C, ldc,
+                                 reinterpret_cast<cudaStream_t>(stream), "bm_sgbmm_db");
 }

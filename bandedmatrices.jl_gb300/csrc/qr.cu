@@ -22,6 +22,7 @@
 // gbqr_lmul: Q or Q' times B, one thread per right-hand side column running the
 // reference loop (sequential fma dot products, so again bit for bit).
 #include "lu.cuh"
+#include "tri.cuh"
 
 namespace bm {
 
@@ -298,10 +299,9 @@ static int tbsv_impl(char uplo, char trans, char diag, i64 n, i64 k, const T* A,
   if (lda < k + 1) return -7;
   if (incx == 0) return -9;
   if (n == 0) return BM_OK;
-  if (!upper || diag == 'U' || diag == 'u' || incx != 1) {
-    set_error("%s: only uplo='U', diag='N', incx=1 are implemented (the banded QR back-substitution)", name);
-    return BM_ERR_UNSUPPORTED;
-  }
+  // lower, unit-diagonal or strided forms: the general one-warp sweep (tri.cu)
+  if (!upper || diag == 'U' || diag == 'u' || incx != 1)
+    return tbsv_general<T>(uplo, trans, diag, n, k, A, lda, x, incx, stream, name);
   const i64 bytes = gbtrs_smem_elems(0, (int)k) * (i64)sizeof(T);
   if (bytes > 227 * 1024) {
     set_error("%s: band too wide for the staged solve", name);

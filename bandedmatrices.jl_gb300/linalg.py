@@ -98,10 +98,8 @@ def mul(A: BandedMatrix, X):
         y = torch.empty(A.m, dtype=A.dtype, device=A.device)
         return mul_(y, A, X, 1.0, 0.0)
     if X.dim() == 2:
-        Y = torch.empty(A.m, X.shape[1], dtype=A.dtype, device=A.device)
-        for k in range(X.shape[1]):
-            mul_(Y[:, k], A, X[:, k].contiguous(), 1.0, 0.0)
-        return Y
+        from .tri import _empty_colmajor, gbmm_dense_
+        return gbmm_dense_(_empty_colmajor(A.m, X.shape[1], X), A, X, 1.0, 0.0)
     raise TypeError("unsupported operand")
 
 

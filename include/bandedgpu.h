@@ -143,13 +143,45 @@ int bm_dgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const 
 int bm_sgbqr_lmul(char trans, int64_t m, int64_t n, int64_t l, int64_t u, const float *AB, int64_t ldab,
                   const float *tau, int64_t ntau, int64_t nrhs, float *B, int64_t ldb, bm_stream_t stream);
 
-/* Triangular band solve op(A) x = b, BLAS xTBSV; uplo 'U', diag 'N', incx 1 (the
- * case banded QR's back-substitution uses).  Replaces tbsv! (src/blas.jl:112-147)
- * reached from UpperTriangular(R) \ b (src/tribanded.jl:75-83). */
+/* Triangular band solve x <- op(A)^-1 x, BLAS xTBSV: uplo 'U'/'L', trans 'N'/'T'/'C',
+ * diag 'N'/'U', any nonzero incx (negative: BLAS convention); A is the triangular band
+ * (k+1) x n with lda >= k+1 (upper: diagonal in row k; lower: diagonal in row 0).  Each
+ * element gets reference DTBSV's operations in its order (fused multiply-adds).
+ * Replaces tbsv! (src/blas.jl:112-147) reached from UpperTriangular(A) \ b and
+ * LowerTriangular(A) \ b (src/tribanded.jl:75-96), and banded QR's back-substitution. */
 int bm_dtbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const double *A, int64_t lda, double *x,
              int64_t incx, bm_stream_t stream);
 int bm_stbsv(char uplo, char trans, char diag, int64_t n, int64_t k, const float *A, int64_t lda, float *x,
              int64_t incx, bm_stream_t stream);
+
+/* Triangular band product x <- op(A) x, BLAS xTBMV, every uplo / trans / diag form,
+ * any nonzero incx; storage as xTBSV.  Each output gets reference DTBMV's operations in
+ * its order.  Replaces tbmv! (src/blas.jl:71-108) reached from UpperTriangular(A) * x
+ * and LowerTriangular(A) * x (src/tribanded.jl:47-54). */
+int bm_dtbmv(char uplo, char trans, char diag, int64_t n, int64_t k, const double *A, int64_t lda, double *x,
+             int64_t incx, bm_stream_t stream);
+int bm_stbmv(char uplo, char trans, char diag, int64_t n, int64_t k, const float *A, int64_t lda, float *x,
+             int64_t incx, bm_stream_t stream);
+
+/* Banded x dense: C <- alpha*A*B + beta*C for banded A (m x n, bandwidths (kl,ku),
+ * lda >= kl+ku+1), dense B (n x k, ldb >= max(1,n)) and C (m x k, ldc >= max(1,m));
+ * column c of C equals xGBMV 'N' of A with column c of B, bit for bit (the column loop
+ * of materialize!(::MatMulMatAdd{<:BandedColumns,<:AbstractStridedLayout}),
+ * src/generic/matmul.jl:243-256).  beta == 0: C is not read. */
+int bm_dgbmm_bd(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, double alpha, const double *A, int64_t lda,
+                const double *B, int64_t ldb, double beta, double *C, int64_t ldc, bm_stream_t stream);
+int bm_sgbmm_bd(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, float alpha, const float *A, int64_t lda,
+                const float *B, int64_t ldb, float beta, float *C, int64_t ldc, bm_stream_t stream);
+
+/* Dense x banded: C <- alpha*D*A + beta*C for dense D (k x m, ldd >= max(1,k)),
+ * banded A (m x n, (kl,ku), lda) and C (k x n, ldc >= max(1,k)); row r of C equals
+ * xGBMV 'T' of A with row r of D, bit for bit (the row loop of
+ * materialize!(::MatMulMatAdd{<:AbstractStridedLayout,<:BandedColumns}),
+ * src/generic/matmul.jl:258-271). */
+int bm_dgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, double alpha, const double *D, int64_t ldd,
+                const double *A, int64_t lda, double beta, double *C, int64_t ldc, bm_stream_t stream);
+int bm_sgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, float alpha, const float *D, int64_t ldd,
+                const float *A, int64_t lda, float beta, float *C, int64_t ldc, bm_stream_t stream);
 
 /* ------------------------------------------------------------------ adjoint
  * Reverse-mode derivative of X = A \ B for an upstream gradient W = dL/dX (all

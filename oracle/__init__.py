@@ -9,7 +9,7 @@ imports it.
   * reference BLAS/LAPACK routines that BandedMatrices.jl ccalls
     (``dgbmv`` src/blas.jl:19-26 and src/generic/matmul.jl:22, ``dgbtrf``
     src/banded/BandedLU.jl:98, ``dgbtrs`` src/banded/linalg.jl:28,46,
-    ``dtbsv`` src/blas.jl:134);
+    ``dtbsv`` src/blas.jl:134, ``dtbmv`` src/blas.jl:94);
   * the reference's own Julia loops ``_gbmm!`` (src/banded/gbmm.jl:296-340),
     ``banded_mul!`` (src/generic/matmul.jl:143-172), ``_banded_qr!``
     (src/banded/bandedqr.jl:13-28) and ``banded_qr_lmul!``
@@ -55,6 +55,7 @@ def lib() -> ctypes.CDLL:
             getattr(L, f"or_{p}gbmv").argtypes = [c, i64, i64, i64, i64, T, P, i64, P, i64, T, P, i64]
             getattr(L, f"or_{p}gbtf2").argtypes = [i64, i64, i64, i64, P, i64, P, P]
             getattr(L, f"or_{p}tbsv").argtypes = [c, c, c, i64, i64, P, i64, P]
+            getattr(L, f"or_{p}tbmv").argtypes = [c, c, c, i64, i64, P, i64, P]
             getattr(L, f"or_{p}gbtrs").argtypes = [c, i64, i64, i64, i64, P, i64, P, P, i64]
             getattr(L, f"or_{p}gbmm_generic").argtypes = [i64] * 9 + [T, P, i64, P, i64, T, P, i64]
             getattr(L, f"or_{p}gbmm_percol").argtypes = [i64] * 7 + [T, P, i64, P, i64, T, P, i64]
@@ -134,6 +135,16 @@ def tbsv(uplo, trans, diag, n, k, A, x):
     x = np.array(x, dtype=A.dtype, copy=True)
     st = getattr(lib(), f"or_{p}tbsv")(uplo.encode(), trans.encode(), diag.encode(), n, k, _ptr(A), A.shape[0], _ptr(x))
     _check(st, "tbsv")
+    return x
+
+
+def tbmv(uplo, trans, diag, n, k, A, x):
+    """x <- op(A) x for a triangular band (xTBMV); returns a new array."""
+    A = np.asfortranarray(A)
+    p = _pfx(A)
+    x = np.array(x, dtype=A.dtype, copy=True)
+    st = getattr(lib(), f"or_{p}tbmv")(uplo.encode(), trans.encode(), diag.encode(), n, k, _ptr(A), A.shape[0], _ptr(x))
+    _check(st, "tbmv")
     return x
 
 

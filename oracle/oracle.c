@@ -404,6 +404,64 @@ int P##gbqr_lmul(char trans, i64 m, i64 n, i64 l, i64 u, const T *D, i64 ldd, co
 DEFINE_ALL(double, or_d, fma, fabs, sqrt, copysign)
 DEFINE_ALL(float, or_s, fmaf, fabsf, sqrtf, copysignf)
 
+/* Reference BLAS xTBMV (x := op(A) x, A a triangular band with k off-diagonals in BLAS
+ * triangular band storage), upper/lower, 'N'/'T', unit/non-unit, incx = 1: the loop
+ * order of reference DTBMV (tbmv!, src/blas.jl:71-108), each multiply-add fused. */
+#define DEFINE_TBMV(T, P, FMA)                                                                  \
+int P##tbmv(char uplo, char trans, char diag, i64 n, i64 k, const T *a, i64 lda, T *x)          \
+{                                                                                               \
+    int upper = (uplo == 'U' || uplo == 'u');                                                   \
+    int notr = (trans == 'N' || trans == 'n');                                                  \
+    int nounit = (diag == 'N' || diag == 'n');                                                  \
+    if (n < 0) return -4;                                                                       \
+    if (k < 0) return -5;                                                                       \
+    if (lda < k + 1) return -7;                                                                 \
+    if (n == 0) return 0;                                                                       \
+    if (notr) {                                                                                 \
+        if (upper) {                                                                            \
+            for (i64 j = 0; j < n; j++) {                                                       \
+                if (x[j] != 0) {                                                                \
+                    T temp = x[j];                                                              \
+                    for (i64 i = imax(0, j - k); i < j; i++)                                    \
+                        x[i] = FMA(temp, a[(k - j + i) + j * lda], x[i]);                       \
+                    if (nounit) x[j] = x[j] * a[k + j * lda];                                   \
+                }                                                                               \
+            }                                                                                   \
+        } else {                                                                                \
+            for (i64 j = n - 1; j >= 0; j--) {                                                  \
+                if (x[j] != 0) {                                                                \
+                    T temp = x[j];                                                              \
+                    for (i64 i = imin(n - 1, j + k); i > j; i--)                                \
+                        x[i] = FMA(temp, a[(i - j) + j * lda], x[i]);                           \
+                    if (nounit) x[j] = x[j] * a[0 + j * lda];                                   \
+                }                                                                               \
+            }                                                                                   \
+        }                                                                                       \
+    } else {                                                                                    \
+        if (upper) {                                                                            \
+            for (i64 j = n - 1; j >= 0; j--) {                                                  \
+                T temp = x[j];                                                                  \
+                if (nounit) temp = temp * a[k + j * lda];                                       \
+                for (i64 i = j - 1; i >= imax(0, j - k); i--)                                   \
+                    temp = FMA(a[(k - j + i) + j * lda], x[i], temp);                           \
+                x[j] = temp;                                                                    \
+            }                                                                                   \
+        } else {                                                                                \
+            for (i64 j = 0; j < n; j++) {                                                       \
+                T temp = x[j];                                                                  \
+                if (nounit) temp = temp * a[0 + j * lda];                                       \
+                for (i64 i = j + 1; i <= imin(n - 1, j + k); i++)                               \
+                    temp = FMA(a[(i - j) + j * lda], x[i], temp);                               \
+                x[j] = temp;                                                                    \
+            }                                                                                   \
+        }                                                                                       \
+    }                                                                                           \
+    return 0;                                                                                   \
+}
+
+DEFINE_TBMV(double, or_d, fma)
+DEFINE_TBMV(float, or_s, fmaf)
+
 /* Adjoint of x = A \ b with L = w.x (the rrule of \): lambda = A^{-T} w via the
  * transposed xGBTRS on the stored factors; dL/db = lambda; dL/dA(i,j) = -lambda_i x_j on
  * the band of A (BLAS band storage, (kl+ku+1) x n, leading dim ldg). */

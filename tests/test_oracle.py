@@ -250,3 +250,34 @@ def test_gbtf2_blocked_regime_golden(orc, name):
     r = orc.gbmv("N", n, n, l, u, 1.0, data, x) - b
     rowsum = orc.gbmv("N", n, n, l, u, 1.0, np.abs(data), np.ones(n))
     assert np.abs(r).max() / (rowsum.max() * np.abs(x).max() + np.abs(b).max()) <= 1e-12
+
+
+NEXT = os.path.join(os.path.dirname(__file__), "golden", "next_golden.npz")
+TRI_FORMS = [(u, t, d) for u in "UL" for t in "NT" for d in "NU"]
+
+
+def test_tbmv_tbsv_every_form_golden(orc):
+    """The xTBMV / xTBSV restatements against OpenBLAS dtbmv / dtbsv in all eight
+    uplo / trans / diag forms (OpenBLAS's kernels may sum in another order: 1e-13)."""
+    gn = np.load(NEXT)
+    for c in range(2):
+        n, k = (int(v) for v in gn[f"tri{c}_dims"])
+        for u, t, d in TRI_FORMS:
+            key = f"tri{c}_{u}{t}{d}"
+            A, x = gn[key + "_A"], gn[key + "_x"]
+            assert _rel(orc.tbmv(u, t, d, n, k, A, x), gn[key + "_mv"]) < 1e-13, key
+            assert _rel(orc.tbsv(u, t, d, n, k, A, x), gn[key + "_sv"]) < 1e-13, key
+
+
+def test_banded_dense_products_golden(orc):
+    """Banded x dense (a gbmv 'N' per column) and dense x banded (a gbmv 'T' per row)
+    against the same loops over OpenBLAS dgbmv."""
+    gn = np.load(NEXT)
+    for c in range(2):
+        m, n, kl, ku, k = (int(v) for v in gn[f"bd{c}_dims"])
+        alpha, beta = gn[f"bd{c}_ab"]
+        A, B, C0, D, E0 = (gn[f"bd{c}_{s}"] for s in ("A", "B", "C0", "D", "E0"))
+        C = np.stack([orc.gbmv("N", m, n, kl, ku, alpha, A, B[:, j], beta, C0[:, j]) for j in range(k)], axis=1)
+        E = np.stack([orc.gbmv("T", m, n, kl, ku, alpha, A, D[r, :], beta, E0[r, :]) for r in range(k)], axis=0)
+        assert np.array_equal(C, gn[f"bd{c}_C"]), c  # the 'N' loop is OpenBLAS's order
+        assert _rel(E, gn[f"bd{c}_E"]) < 1e-14, c
