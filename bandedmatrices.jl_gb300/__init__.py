@@ -20,6 +20,7 @@ from .autograd import BandedSolve, banded_solve
 from .refine import solve_refined
 from .tri import (LowerTriangular, UnitLowerTriangular, UnitUpperTriangular, UpperTriangular, dense_gbmm_,
                   gbmm_dense_)
+from .symbanded import BandedCholesky, Symmetric, cholesky
 from . import pde, shard
 
 __all__ = [
@@ -28,7 +29,7 @@ __all__ = [
     "banded_mul", "banded_mul_", "gbmm", "nonzero_bands", "prodbandwidths",
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
     "solve_refined", "UpperTriangular", "LowerTriangular", "UnitUpperTriangular", "UnitLowerTriangular",
-    "gbmm_dense_", "dense_gbmm_",
+    "gbmm_dense_", "dense_gbmm_", "Symmetric", "BandedCholesky", "cholesky",
     "BandedSolve", "banded_solve",
 ]
 

@@ -54,6 +54,12 @@ SIGNATURES: dict[str, list] = {
     "bm_stbsv": [C, C, C, i64, i64, P, i64, P, i64, P],
     "bm_dtbmv": [C, C, C, i64, i64, P, i64, P, i64, P],
     "bm_stbmv": [C, C, C, i64, i64, P, i64, P, i64, P],
+    "bm_dpbtrf": [C, i64, i64, P, i64, P, P],
+    "bm_spbtrf": [C, i64, i64, P, i64, P, P],
+    "bm_dpbtrs": [C, i64, i64, i64, P, i64, P, i64, P],
+    "bm_spbtrs": [C, i64, i64, i64, P, i64, P, i64, P],
+    "bm_dsbmv": [C, i64, i64, D, P, i64, P, i64, D, P, i64, P],
+    "bm_ssbmv": [C, i64, i64, F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm_bd": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmm_bd": [i64] * 5 + [F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm_db": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],

@@ -17,7 +17,7 @@
 // overwritten it (the 'ahead' forms -- N/U and T/L read x(i .. i+k) -- ascending,
 // the others descending); inside a tile every thread computes its output from the old
 // values, the CTA synchronises, then the tile is written.
-#include "common.cuh"
+#include "tri.cuh"
 
 namespace bm {
 
@@ -29,8 +29,8 @@ struct StridedVec {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(32) tbsv_warp_kernel(bool upper, bool trans, bool unit, i64 n, int k,
-                                                       const T* __restrict__ A, i64 lda, T* x, i64 incx) {
+__device__ void tbsv_warp(bool upper, bool trans, bool unit, i64 n, int k, const T* __restrict__ A, i64 lda, T* x,
+                          i64 incx) {
   const int lane = threadIdx.x & 31;
   const StridedVec<T> X{x, incx, incx > 0 ? 0 : -(n - 1) * incx};
   if (!trans) {
@@ -74,6 +74,14 @@ __global__ void __launch_bounds__(32) tbsv_warp_kernel(bool upper, bool trans, b
       __syncwarp();
     }
   }
+}
+
+// Vector v = blockIdx.x (grid-stride) of nvec, at x + v * ldx.
+template <typename T>
+__global__ void __launch_bounds__(32) tbsv_warp_kernel(bool upper, bool trans, bool unit, i64 n, int k,
+                                                       const T* __restrict__ A, i64 lda, T* x, i64 incx, i64 nvec,
+                                                       i64 ldx) {
+  for (i64 v = blockIdx.x; v < nvec; v += gridDim.x) tbsv_warp(upper, trans, unit, n, k, A, lda, x + v * ldx, incx);
 }
 
 constexpr int kTbmvThreads = 256;
@@ -138,18 +146,20 @@ static int tri_check(char uplo, char trans, char diag, i64 n, i64 k, i64 lda, i6
 
 template <typename T>
 int tbsv_general(char uplo, char trans, char diag, i64 n, i64 k, const T* A, i64 lda, T* x, i64 incx,
-                 cudaStream_t stream, const char* name) {
+                 cudaStream_t stream, const char* name, i64 nvec, i64 ldx) {
   if (int r = tri_check(uplo, trans, diag, n, k, lda, incx)) return r;
-  if (n == 0) return BM_OK;
+  if (n == 0 || nvec == 0) return BM_OK;
   if (k > 0x7fffffff) return -5;
-  tbsv_warp_kernel<T><<<1, 32, 0, stream>>>(uplo == 'U' || uplo == 'u', !(trans == 'N' || trans == 'n'),
-                                            diag == 'U' || diag == 'u', n, (int)k, A, lda, x, incx);
+  const i64 grid = std::min<i64>(nvec, (i64)num_sms() * 16);
+  tbsv_warp_kernel<T><<<(unsigned)grid, 32, 0, stream>>>(uplo == 'U' || uplo == 'u', !(trans == 'N' || trans == 'n'),
+                                                         diag == 'U' || diag == 'u', n, (int)k, A, lda, x, incx, nvec,
+                                                         ldx);
   return launch_status(name);
 }
 template int tbsv_general<double>(char, char, char, i64, i64, const double*, i64, double*, i64, cudaStream_t,
-                                  const char*);
+                                  const char*, i64, i64);
 template int tbsv_general<float>(char, char, char, i64, i64, const float*, i64, float*, i64, cudaStream_t,
-                                 const char*);
+                                 const char*, i64, i64);
 
 template <typename T>
 static int tbmv_impl(char uplo, char trans, char diag, i64 n, i64 k, const T* A, i64 lda, T* x, i64 incx,

@@ -183,6 +183,34 @@ int bm_dgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, double 
 int bm_sgbmm_db(int64_t m, int64_t n, int64_t kl, int64_t ku, int64_t k, float alpha, const float *D, int64_t ldd,
                 const float *A, int64_t lda, float beta, float *C, int64_t ldc, bm_stream_t stream);
 
+/* ------------------------------------------------------------------ symmetric band
+ * Cholesky factorization of a symmetric positive definite band, LAPACK xPBTRF: AB is
+ * the (kd+1) x n symmetric band storage (uplo 'U': A(i,j) at row kd+i-j for i <= j;
+ * 'L': at row i-j for i >= j), ldab >= kd+1, overwritten by the factor U (A = U^T U) or
+ * L (A = L L^T); *info (device) receives 0, or j > 0 when the leading minor of order j
+ * is not positive definite (the factorization stops there).  Element for element the
+ * unblocked xPBTF2 (bit for bit with it); kd <= 167 in Float64, 237 in Float32.
+ * Replaces pbtrf! (src/lapack.jl:268-298) reached from banded_chol!
+ * (src/symbanded/BandedCholesky.jl:2-12). */
+int bm_dpbtrf(char uplo, int64_t n, int64_t kd, double *AB, int64_t ldab, int64_t *info, bm_stream_t stream);
+int bm_spbtrf(char uplo, int64_t n, int64_t kd, float *AB, int64_t ldab, int64_t *info, bm_stream_t stream);
+
+/* Solve A X = B with the xPBTRF factor (LAPACK xPBTRS: two triangular band sweeps per
+ * right-hand side); B is n x nrhs, ldb >= max(1,n), overwritten with X.  Replaces
+ * pbtrs! (src/lapack.jl:300-332). */
+int bm_dpbtrs(char uplo, int64_t n, int64_t kd, int64_t nrhs, const double *AB, int64_t ldab, double *B, int64_t ldb,
+              bm_stream_t stream);
+int bm_spbtrs(char uplo, int64_t n, int64_t kd, int64_t nrhs, const float *AB, int64_t ldab, float *B, int64_t ldb,
+              bm_stream_t stream);
+
+/* y <- alpha*A*x + beta*y for a symmetric band A (k off-diagonals, storage as xPBTRF's),
+ * BLAS xSBMV, any nonzero incx/incy; each output in reference DSBMV's order.  Replaces
+ * sbmv! (src/blas.jl:35-64). */
+int bm_dsbmv(char uplo, int64_t n, int64_t k, double alpha, const double *A, int64_t lda, const double *x,
+             int64_t incx, double beta, double *y, int64_t incy, bm_stream_t stream);
+int bm_ssbmv(char uplo, int64_t n, int64_t k, float alpha, const float *A, int64_t lda, const float *x, int64_t incx,
+             float beta, float *y, int64_t incy, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ adjoint
  * Reverse-mode derivative of X = A \ B for an upstream gradient W = dL/dX (all
  * n x nrhs, leading dim n), with A's xGBTRF factors (LU, ldab, ipiv):

@@ -56,6 +56,9 @@ def lib() -> ctypes.CDLL:
             getattr(L, f"or_{p}gbtf2").argtypes = [i64, i64, i64, i64, P, i64, P, P]
             getattr(L, f"or_{p}tbsv").argtypes = [c, c, c, i64, i64, P, i64, P]
             getattr(L, f"or_{p}tbmv").argtypes = [c, c, c, i64, i64, P, i64, P]
+            getattr(L, f"or_{p}pbtf2").argtypes = [c, i64, i64, P, i64, P]
+            getattr(L, f"or_{p}pbtrs").argtypes = [c, i64, i64, i64, P, i64, P, i64]
+            getattr(L, f"or_{p}sbmv").argtypes = [c, i64, i64, T, P, i64, P, T, P]
             getattr(L, f"or_{p}gbtrs").argtypes = [c, i64, i64, i64, i64, P, i64, P, P, i64]
             getattr(L, f"or_{p}gbmm_generic").argtypes = [i64] * 9 + [T, P, i64, P, i64, T, P, i64]
             getattr(L, f"or_{p}gbmm_percol").argtypes = [i64] * 7 + [T, P, i64, P, i64, T, P, i64]
@@ -146,6 +149,40 @@ def tbmv(uplo, trans, diag, n, k, A, x):
     st = getattr(lib(), f"or_{p}tbmv")(uplo.encode(), trans.encode(), diag.encode(), n, k, _ptr(A), A.shape[0], _ptr(x))
     _check(st, "tbmv")
     return x
+
+
+def pbtf2(uplo, n, kd, AB):
+    """Unblocked banded Cholesky (xPBTF2) on a copy of AB ((kd+1) x n symmetric band
+    storage).  Returns (factor, info)."""
+    F = _fortran(AB)
+    p = _pfx(F)
+    info = ctypes.c_int64(0)
+    st = getattr(lib(), f"or_{p}pbtf2")(uplo.encode(), n, kd, _ptr(F), F.shape[0], ctypes.byref(info))
+    _check(st, "pbtf2")
+    return F, int(info.value)
+
+
+def pbtrs(uplo, n, kd, F, B):
+    """xPBTRS with the Cholesky factor F; B is (n,) or (n, nrhs).  Returns the solution."""
+    F = np.asfortranarray(F)
+    p = _pfx(F)
+    vec = B.ndim == 1
+    X = _fortran(B.reshape(n, -1), F.dtype)
+    st = getattr(lib(), f"or_{p}pbtrs")(uplo.encode(), n, kd, X.shape[1], _ptr(F), F.shape[0], _ptr(X), max(1, n))
+    _check(st, "pbtrs")
+    return X[:, 0].copy() if vec else X
+
+
+def sbmv(uplo, n, k, alpha, A, x, beta=0.0, y=None):
+    """y <- alpha A x + beta y for a symmetric band A ((k+1) x n, xSBMV); returns a new array."""
+    A = np.asfortranarray(A)
+    p = _pfx(A)
+    T = A.dtype.type
+    x = np.ascontiguousarray(x, dtype=A.dtype)
+    y = np.zeros(n, dtype=A.dtype) if y is None else np.array(y, dtype=A.dtype, copy=True)
+    st = getattr(lib(), f"or_{p}sbmv")(uplo.encode(), n, k, T(alpha), _ptr(A), A.shape[0], _ptr(x), T(beta), _ptr(y))
+    _check(st, "sbmv")
+    return y
 
 
 def gbmm_generic(n, nu, m, Al, Au, Bl, Bu, Cl, Cu, alpha, A, B, beta, C):

@@ -462,6 +462,120 @@ int P##tbmv(char uplo, char trans, char diag, i64 n, i64 k, const T *a, i64 lda,
 DEFINE_TBMV(double, or_d, fma)
 DEFINE_TBMV(float, or_s, fmaf)
 
+/* Symmetric positive definite band: LAPACK xPBTF2 (unblocked Cholesky, the loop order of
+ * dpbtf2: sqrt of the pivot, dscal of the row (upper) or column (lower) by its
+ * reciprocal, dsyr rank-1 update of the trailing kn x kn triangle with each element
+ * a <- fma(x_i, -x_j, a), column j skipped when x_j == 0), xPBTRS (two xTBSV sweeps)
+ * and reference BLAS xSBMV (y := alpha A x + beta y, A symmetric band).  pbtrf!/pbtrs!
+ * src/lapack.jl:268-332 (banded_chol!, src/symbanded/BandedCholesky.jl:2-12);
+ * sbmv! src/blas.jl:35-64. */
+#define DEFINE_SYMBAND(T, P, FMA, SQRT)                                                         \
+int P##pbtf2(char uplo, i64 n, i64 kd, T *ab, i64 ldab, i64 *info)                             \
+{                                                                                               \
+    int upper = (uplo == 'U' || uplo == 'u');                                                   \
+    *info = 0;                                                                                  \
+    if (!upper && !(uplo == 'L' || uplo == 'l')) return -1;                                     \
+    if (n < 0) return -2;                                                                       \
+    if (kd < 0) return -3;                                                                      \
+    if (ldab < kd + 1) return -5;                                                               \
+    for (i64 j = 0; j < n; j++) {                                                               \
+        T *d = ab + (upper ? kd : 0) + j * ldab;                                                \
+        T ajj = *d;                                                                             \
+        if (!(ajj > 0)) { *info = j + 1; return 0; }                                            \
+        ajj = SQRT(ajj);                                                                        \
+        *d = ajj;                                                                               \
+        i64 kn = imin(kd, n - 1 - j);                                                           \
+        if (kn > 0) {                                                                           \
+            T r = (T)1 / ajj;                                                                   \
+            /* x_t = A(j, j+t) (upper, along the row) or A(j+t, j) (lower, down the column) */   \
+            for (i64 t = 1; t <= kn; t++) {                                                     \
+                T *p = upper ? ab + (kd - t) + (j + t) * ldab : ab + t + j * ldab;              \
+                *p = r * *p;                                                                    \
+            }                                                                                   \
+            for (i64 c = 1; c <= kn; c++) {                                                     \
+                if (upper) {                                                                    \
+                    T xc = ab[(kd - c) + (j + c) * ldab];                                       \
+                    if (xc != 0) {                                                              \
+                        T temp = -xc;                                                           \
+                        for (i64 s = 1; s <= c; s++) {                                          \
+                            T xs = ab[(kd - s) + (j + s) * ldab];                               \
+                            T *a = ab + (kd + s - c) + (j + c) * ldab;                          \
+                            *a = FMA(xs, temp, *a);                                             \
+                        }                                                                       \
+                    }                                                                           \
+                } else {                                                                        \
+                    T xc = ab[c + j * ldab];                                                    \
+                    if (xc != 0) {                                                              \
+                        T temp = -xc;                                                           \
+                        for (i64 s = c; s <= kn; s++) {                                         \
+                            T xs = ab[s + j * ldab];                                            \
+                            T *a = ab + (s - c) + (j + c) * ldab;                               \
+                            *a = FMA(xs, temp, *a);                                             \
+                        }                                                                       \
+                    }                                                                           \
+                }                                                                               \
+            }                                                                                   \
+        }                                                                                       \
+    }                                                                                           \
+    return 0;                                                                                   \
+}                                                                                               \
+                                                                                                \
+int P##pbtrs(char uplo, i64 n, i64 kd, i64 nrhs, const T *ab, i64 ldab, T *b, i64 ldb)         \
+{                                                                                               \
+    int upper = (uplo == 'U' || uplo == 'u');                                                   \
+    if (!upper && !(uplo == 'L' || uplo == 'l')) return -1;                                     \
+    if (n < 0) return -2;                                                                       \
+    if (kd < 0) return -3;                                                                      \
+    if (nrhs < 0) return -4;                                                                    \
+    if (ldab < kd + 1) return -6;                                                               \
+    if (ldb < imax(1, n)) return -8;                                                            \
+    for (i64 r = 0; r < nrhs; r++) {                                                            \
+        if (upper) {                                                                            \
+            P##tbsv('U', 'T', 'N', n, kd, ab, ldab, b + r * ldb);                               \
+            P##tbsv('U', 'N', 'N', n, kd, ab, ldab, b + r * ldb);                               \
+        } else {                                                                                \
+            P##tbsv('L', 'N', 'N', n, kd, ab, ldab, b + r * ldb);                               \
+            P##tbsv('L', 'T', 'N', n, kd, ab, ldab, b + r * ldb);                               \
+        }                                                                                       \
+    }                                                                                           \
+    return 0;                                                                                   \
+}                                                                                               \
+                                                                                                \
+int P##sbmv(char uplo, i64 n, i64 k, T alpha, const T *a, i64 lda, const T *x, T beta, T *y)    \
+{                                                                                               \
+    int upper = (uplo == 'U' || uplo == 'u');                                                   \
+    if (!upper && !(uplo == 'L' || uplo == 'l')) return -1;                                     \
+    if (n < 0) return -2;                                                                       \
+    if (k < 0) return -3;                                                                       \
+    if (lda < k + 1) return -6;                                                                 \
+    if (n == 0 || (alpha == 0 && beta == 1)) return 0;                                          \
+    if (beta != 1)                                                                              \
+        for (i64 i = 0; i < n; i++) y[i] = (beta == 0) ? (T)0 : beta * y[i];                    \
+    if (alpha == 0) return 0;                                                                   \
+    for (i64 j = 0; j < n; j++) {                                                               \
+        T temp1 = alpha * x[j], temp2 = 0;                                                      \
+        if (upper) {                                                                            \
+            for (i64 i = imax(0, j - k); i < j; i++) {                                          \
+                y[i] = FMA(temp1, a[(k - j + i) + j * lda], y[i]);                              \
+                temp2 = FMA(a[(k - j + i) + j * lda], x[i], temp2);                             \
+            }                                                                                   \
+            y[j] = FMA(temp1, a[k + j * lda], y[j]);                                            \
+            y[j] = FMA(alpha, temp2, y[j]);                                                     \
+        } else {                                                                                \
+            y[j] = FMA(temp1, a[0 + j * lda], y[j]);                                            \
+            for (i64 i = j + 1; i <= imin(n - 1, j + k); i++) {                                 \
+                y[i] = FMA(temp1, a[(i - j) + j * lda], y[i]);                                  \
+                temp2 = FMA(a[(i - j) + j * lda], x[i], temp2);                                 \
+            }                                                                                   \
+            y[j] = FMA(alpha, temp2, y[j]);                                                     \
+        }                                                                                       \
+    }                                                                                           \
+    return 0;                                                                                   \
+}
+
+DEFINE_SYMBAND(double, or_d, fma, sqrt)
+DEFINE_SYMBAND(float, or_s, fmaf, sqrtf)
+
 /* Adjoint of x = A \ b with L = w.x (the rrule of \): lambda = A^{-T} w via the
  * transposed xGBTRS on the stored factors; dL/db = lambda; dL/dA(i,j) = -lambda_i x_j on
  * the band of A (BLAS band storage, (kl+ku+1) x n, leading dim ldg). */

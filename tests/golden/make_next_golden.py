@@ -53,6 +53,21 @@ def main():
         g[f"bd{c}_ab"] = np.array([alpha, beta])
         g[f"bd{c}_A"], g[f"bd{c}_B"], g[f"bd{c}_C0"], g[f"bd{c}_C"] = A, B, C0, C
         g[f"bd{c}_D"], g[f"bd{c}_E0"], g[f"bd{c}_E"] = D, E0, E
+    # symmetric band product and banded Cholesky (a diagonally dominant SPD band)
+    for c, (n, k) in enumerate([(300, 6), (200, 40)]):
+        for u in "UL":
+            key = f"sym{c}_{u}"
+            A = rng.standard_normal((k + 1, n))
+            A[k if u == "U" else 0] = np.abs(A[k if u == "U" else 0]) + 2.0 * (k + 1)
+            x, y0 = rng.standard_normal(n), rng.standard_normal(n)
+            b = rng.standard_normal((n, 2))
+            g[key + "_A"], g[key + "_x"], g[key + "_y0"], g[key + "_b"] = A, x, y0, b
+            g[key + "_sbmv"] = blas.dsbmv(k, 0.7, np.asfortranarray(A), x, beta=-1.5, y=y0.copy(), lower=int(u == "L"))
+            F, info = lapack.dpbtrf(np.asfortranarray(A), lower=int(u == "L"))
+            assert info == 0
+            X, info = lapack.dpbtrs(F, b, lower=int(u == "L"))
+            g[key + "_F"], g[key + "_X"] = F, X
+        g[f"sym{c}_dims"] = np.array([n, k], dtype=np.int64)
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e6:.2f} MB, {len(g)} arrays)")
 

@@ -145,7 +145,7 @@ def test_noalloc_batched_rejects_bad_descriptors(bm, gpu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kl_hi,ku_hi", [(20, 14), (90, 80)])  # blocked FP32 path; group path
+@pytest.mark.parametrize("kl_hi,ku_hi", [(20, 14), (84, 10)])  # blocked FP32 path; group path (kl > 80)
 def test_refined_batched_rejects_bad_descriptors(bm, gpu, kl_hi, ku_hi):
     rng = np.random.default_rng(13)
     batch, bands, rhs = _make(bm, gpu, rng, 24, kl_hi, ku_hi, n_hi=400)

@@ -281,3 +281,22 @@ def test_banded_dense_products_golden(orc):
         E = np.stack([orc.gbmv("T", m, n, kl, ku, alpha, A, D[r, :], beta, E0[r, :]) for r in range(k)], axis=0)
         assert np.array_equal(C, gn[f"bd{c}_C"]), c  # the 'N' loop is OpenBLAS's order
         assert _rel(E, gn[f"bd{c}_E"]) < 1e-14, c
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_pbtf2_pbtrs_sbmv_golden(orc, uplo):
+    """The xPBTF2 / xPBTRS / xSBMV restatements against OpenBLAS dpbtrf / dpbtrs / dsbmv
+    (kd = 6: OpenBLAS's unblocked path; kd = 40: its blocked dpbtrf, same pivots-free
+    result to rounding)."""
+    gn = np.load(NEXT)
+    for c in range(2):
+        n, k = (int(v) for v in gn[f"sym{c}_dims"])
+        key = f"sym{c}_{uplo}"
+        A = gn[key + "_A"]
+        y = orc.sbmv(uplo, n, k, 0.7, A, gn[key + "_x"], -1.5, gn[key + "_y0"])
+        assert _rel(y, gn[key + "_sbmv"]) < 1e-14
+        F, info = orc.pbtf2(uplo, n, k, A)
+        assert info == 0
+        assert _rel(F, gn[key + "_F"]) < 1e-13
+        X = orc.pbtrs(uplo, n, k, F, gn[key + "_b"])
+        assert _rel(X, gn[key + "_X"]) < 1e-13
