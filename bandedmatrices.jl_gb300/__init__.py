@@ -21,6 +21,7 @@ from .refine import solve_refined
 from .tri import (LowerTriangular, UnitLowerTriangular, UnitUpperTriangular, UpperTriangular, dense_gbmm_,
                   gbmm_dense_)
 from .symbanded import BandedCholesky, Symmetric, cholesky
+from .elementwise import add, axpy_, dot, scale_, shift_
 from . import pde, shard
 
 __all__ = [
@@ -30,6 +31,7 @@ __all__ = [
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
     "solve_refined", "UpperTriangular", "LowerTriangular", "UnitUpperTriangular", "UnitLowerTriangular",
     "gbmm_dense_", "dense_gbmm_", "Symmetric", "BandedCholesky", "cholesky",
+    "axpy_", "scale_", "shift_", "add", "dot",
     "BandedSolve", "banded_solve",
 ]
 

@@ -60,6 +60,14 @@ SIGNATURES: dict[str, list] = {
     "bm_spbtrs": [C, i64, i64, i64, P, i64, P, i64, P],
     "bm_dsbmv": [C, i64, i64, D, P, i64, P, i64, D, P, i64, P],
     "bm_ssbmv": [C, i64, i64, F, P, i64, P, i64, F, P, i64, P],
+    "bm_dgbaxpy": [i64, i64, D, i64, i64, P, i64, i64, i64, P, i64, P, P],
+    "bm_sgbaxpy": [i64, i64, F, i64, i64, P, i64, i64, i64, P, i64, P, P],
+    "bm_dgbscal": [i64, i64, i64, i64, D, P, i64, P],
+    "bm_sgbscal": [i64, i64, i64, i64, F, P, i64, P],
+    "bm_dgbshift": [i64, i64, i64, i64, D, P, i64, P],
+    "bm_sgbshift": [i64, i64, i64, i64, F, P, i64, P],
+    "bm_dgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
+    "bm_sgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
     "bm_dgbmm_bd": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmm_bd": [i64] * 5 + [F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm_db": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],

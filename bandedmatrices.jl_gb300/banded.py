@@ -186,6 +186,24 @@ class BandedMatrix:
         from . import linalg
         return linalg.mul(self, other)
 
+    def __add__(self, other):
+        from .elementwise import add
+        return add(self, other, 1.0)
+
+    def __sub__(self, other):
+        from .elementwise import add
+        return add(self, other, -1.0)
+
+    def __neg__(self):
+        from .elementwise import scale_
+        return scale_(-1.0, self.copy())
+
+    def __mul__(self, alpha):
+        from .elementwise import scale_
+        return scale_(float(alpha), self.copy())
+
+    __rmul__ = __mul__
+
     def __rmatmul__(self, D):
         """D * A for a dense D (src/generic/matmul.jl:258-271)."""
         from .tri import _empty_colmajor, dense_gbmm_

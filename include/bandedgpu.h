@@ -211,6 +211,38 @@ int bm_dsbmv(char uplo, int64_t n, int64_t k, double alpha, const double *A, int
 int bm_ssbmv(char uplo, int64_t n, int64_t k, float alpha, const float *A, int64_t lda, const float *x, int64_t incx,
              float beta, float *y, int64_t incy, bm_stream_t stream);
 
+/* ------------------------------------------------------------------ elementwise
+ * Y <- a*X + Y for banded X (m x n, bandwidths (Xl,Xu), ldx) and Y ((Yl,Yu), ldy).
+ * Equal bandwidths: BLAS axpy over the whole storage, y = fma(a, x, y) (axpy!(a, X.data,
+ * Y.data), src/banded/BandedMatrix.jl:1006-1015).  Otherwise banded_generic_axpy!
+ * (src/generic/broadcast.jl:978-1020): *bad (device) receives j*m + k of the first
+ * (column-order) nonzero in-matrix entry X(k,j) outside Y's bands, in which case Y is
+ * left untouched (the reference throws BandError); else *bad = UINT64_MAX and the
+ * overlapping bands get y = a*x + y rounded twice (Julia does not fuse it). */
+int bm_dgbaxpy(int64_t m, int64_t n, double a, int64_t Xl, int64_t Xu, const double *X, int64_t ldx, int64_t Yl,
+               int64_t Yu, double *Y, int64_t ldy, unsigned long long *bad, bm_stream_t stream);
+int bm_sgbaxpy(int64_t m, int64_t n, float a, int64_t Xl, int64_t Xu, const float *X, int64_t ldx, int64_t Yl,
+               int64_t Yu, float *Y, int64_t ldy, unsigned long long *bad, bm_stream_t stream);
+
+/* A <- alpha*A over the band storage (banded_lmul!, src/generic/broadcast.jl:960-965). */
+int bm_dgbscal(int64_t m, int64_t n, int64_t l, int64_t u, double alpha, double *A, int64_t lda, bm_stream_t stream);
+int bm_sgbscal(int64_t m, int64_t n, int64_t l, int64_t u, float alpha, float *A, int64_t lda, bm_stream_t stream);
+
+/* A <- A + sigma*I: sigma added to the min(m,n) diagonal entries (storage row u; needs
+ * l, u >= 0); the broadcast A + sigma*I of src/generic/broadcast.jl in place. */
+int bm_dgbshift(int64_t m, int64_t n, int64_t l, int64_t u, double sigma, double *A, int64_t lda, bm_stream_t stream);
+int bm_sgbshift(int64_t m, int64_t n, int64_t l, int64_t u, float sigma, float *A, int64_t lda, bm_stream_t stream);
+
+/* *result (device) <- dot(x, A, y) = sum_j y_j sum_i A(i,j) x_i for banded A (m x n,
+ * l, u >= 0), x of length m, y of length n; columns with y_j == 0 are skipped as in
+ * _dot (src/banded/dot.jl:1-22).  work: 1024 device elements of scratch.  The column
+ * sums run in ascending i with fused multiply-adds and the total is a fixed two-level
+ * tree: deterministic, equal to the reference's @simd sum to rounding. */
+int bm_dgbdot(int64_t m, int64_t n, int64_t l, int64_t u, const double *x, const double *A, int64_t lda,
+              const double *y, double *result, double *work, bm_stream_t stream);
+int bm_sgbdot(int64_t m, int64_t n, int64_t l, int64_t u, const float *x, const float *A, int64_t lda, const float *y,
+              float *result, float *work, bm_stream_t stream);
+
 /* ------------------------------------------------------------------ adjoint
  * Reverse-mode derivative of X = A \ B for an upstream gradient W = dL/dX (all
  * n x nrhs, leading dim n), with A's xGBTRF factors (LU, ldab, ipiv):

@@ -68,6 +68,32 @@ def main():
             X, info = lapack.dpbtrs(F, b, lower=int(u == "L"))
             g[key + "_F"], g[key + "_X"] = F, X
         g[f"sym{c}_dims"] = np.array([n, k], dtype=np.int64)
+    # axpy!: equal bandwidths is BLAS daxpy over the storage; different bandwidths is
+    # banded_generic_axpy!'s a*x + y on the overlapping bands (NumPy does not fuse); dot
+    for c, (m, n, xl, xu, yl, yu) in enumerate([(90, 90, 3, 4, 3, 4), (80, 100, 2, 5, 6, 1)]):
+        X = rng.standard_normal((xl + xu + 1, n))
+        Y = rng.standard_normal((yl + yu + 1, n))
+        a = -0.625
+        if (xl, xu) == (yl, yu):
+            Z = blas.daxpy(X.ravel(order="F"), Y.ravel(order="F").copy(), a=a).reshape(Y.shape, order="F")
+        else:
+            Z = Y.copy()
+            for j in range(n):
+                for k in range(max(0, j - min(xu, yu)), min(m, j + min(xl, yl) + 1)):
+                    Z[yu + k - j, j] = a * X[xu + k - j, j] + Y[yu + k - j, j]
+            for j in range(n):  # the test keeps X's extra bands zero, as banded_generic_axpy! requires
+                for k in range(max(0, j - xu), min(m, j + xl + 1)):
+                    if not (-yu <= k - j <= yl):
+                        X[xu + k - j, j] = 0.0
+        x, y = rng.standard_normal(m), rng.standard_normal(n)
+        Xd = np.zeros((m, n))
+        for j in range(n):
+            for k in range(max(0, j - xu), min(m, j + xl + 1)):
+                Xd[k, j] = X[xu + k - j, j]
+        g[f"ax{c}_dims"] = np.array([m, n, xl, xu, yl, yu], dtype=np.int64)
+        g[f"ax{c}_a"] = np.array([a])
+        g[f"ax{c}_X"], g[f"ax{c}_Y"], g[f"ax{c}_Z"] = X, Y, Z
+        g[f"ax{c}_x"], g[f"ax{c}_y"], g[f"ax{c}_dot"] = x, y, np.array([x @ (Xd @ y)])
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e6:.2f} MB, {len(g)} arrays)")
 
