@@ -22,6 +22,7 @@ from .tri import (LowerTriangular, UnitLowerTriangular, UnitUpperTriangular, Upp
                   gbmm_dense_)
 from .symbanded import BandedCholesky, Symmetric, cholesky
 from .elementwise import add, axpy_, dot, scale_, shift_
+from .convert import from_rows, from_sparse, sparse, sparse_bandwidths
 from . import pde, shard
 
 __all__ = [
@@ -31,7 +32,7 @@ __all__ = [
     "BandedLU", "ldiv_", "lu", "lu_", "transpose", "BandedBatch", "lpt_order", "BandedQR", "lmul_", "qr",
     "solve_refined", "UpperTriangular", "LowerTriangular", "UnitUpperTriangular", "UnitLowerTriangular",
     "gbmm_dense_", "dense_gbmm_", "Symmetric", "BandedCholesky", "cholesky",
-    "axpy_", "scale_", "shift_", "add", "dot",
+    "axpy_", "scale_", "shift_", "add", "dot", "sparse", "sparse_bandwidths", "from_sparse", "from_rows",
     "BandedSolve", "banded_solve",
 ]
 

@@ -68,6 +68,15 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbshift": [i64, i64, i64, i64, F, P, i64, P],
     "bm_dgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
     "bm_sgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
+    "bm_gb2csc_nnz": [i64, i64, i64, i64],
+    "bm_dgb2csc": [i64, i64, i64, i64, P, i64, P, P, P, P],
+    "bm_sgb2csc": [i64, i64, i64, i64, P, i64, P, P, P, P],
+    "bm_dcsc_bandwidths": [i64, i64, P, P, P, P, P],
+    "bm_scsc_bandwidths": [i64, i64, P, P, P, P, P],
+    "bm_dcsc2gb": [i64, i64, P, P, P, i64, i64, P, i64, P, P],
+    "bm_scsc2gb": [i64, i64, P, P, P, i64, i64, P, i64, P, P],
+    "bm_dgbrows2cols": [i64, i64, i64, i64, P, i64, P, i64, P],
+    "bm_sgbrows2cols": [i64, i64, i64, i64, P, i64, P, i64, P],
     "bm_dgbmm_bd": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
     "bm_sgbmm_bd": [i64] * 5 + [F, P, i64, P, i64, F, P, i64, P],
     "bm_dgbmm_db": [i64] * 5 + [D, P, i64, P, i64, D, P, i64, P],
@@ -107,7 +116,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         fn = getattr(L, name)
         fn.argtypes = argt
         fn.restype = (ctypes.c_char_p if name == "bm_last_error"
-                      else ctypes.c_ulonglong if name == "bm_launch_count" else ctypes.c_int)
+                      else ctypes.c_ulonglong if name == "bm_launch_count"
+                      else ctypes.c_int64 if name == "bm_gb2csc_nnz" else ctypes.c_int)
     _lib = L
     return L
 

@@ -243,6 +243,45 @@ int bm_dgbdot(int64_t m, int64_t n, int64_t l, int64_t u, const double *x, const
 int bm_sgbdot(int64_t m, int64_t n, int64_t l, int64_t u, const float *x, const float *A, int64_t lda, const float *y,
               float *result, float *work, bm_stream_t stream);
 
+/* ------------------------------------------------------------------ conversion
+ * sparse(A) for an m x n band (l, u) as CSC arrays on the device: colptr (n+1 int64,
+ * 0-based), rowval and nzval (bm_gb2csc_nnz(m, n, l, u) entries).  Every in-matrix band
+ * slot is a stored entry (zeros included); a column without one keeps one structural
+ * zero at the clamped row, as sparse(_banded_rowval, _banded_colval, _banded_nzval)
+ * builds it (ext/BandedMatricesSparseArraysExt.jl:7-9, src/banded/BandedMatrix.jl:
+ * 796-836). */
+int64_t bm_gb2csc_nnz(int64_t m, int64_t n, int64_t l, int64_t u);
+int bm_dgb2csc(int64_t m, int64_t n, int64_t l, int64_t u, const double *A, int64_t lda, int64_t *colptr,
+               int64_t *rowval, double *nzval, bm_stream_t stream);
+int bm_sgb2csc(int64_t m, int64_t n, int64_t l, int64_t u, const float *A, int64_t lda, int64_t *colptr,
+               int64_t *rowval, float *nzval, bm_stream_t stream);
+
+/* lu[0], lu[1] (device) <- bandwidths(S) of a CSC matrix (m x n; colptr/rowval 0-based):
+ * the extreme diagonals of its nonzero values, -max(m,n) each when every stored value is
+ * zero, -40320 each (bandwidths(Zeros)) when nothing is stored (the extension's
+ * bandwidths(::SparseMatrixCSC), ext/BandedMatricesSparseArraysExt.jl:11-33). */
+int bm_dcsc_bandwidths(int64_t m, int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
+                       int64_t *lu, bm_stream_t stream);
+int bm_scsc_bandwidths(int64_t m, int64_t n, const int64_t *colptr, const int64_t *rowval, const float *nzval,
+                       int64_t *lu, bm_stream_t stream);
+
+/* BandedMatrix(S, (l, u)): the band storage A ((l+u+1) x n, lda) zeroed and filled from
+ * the CSC matrix S; *dropped (device) counts nonzero entries outside the band (not
+ * stored). */
+int bm_dcsc2gb(int64_t m, int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval, int64_t l,
+               int64_t u, double *A, int64_t lda, unsigned long long *dropped, bm_stream_t stream);
+int bm_scsc2gb(int64_t m, int64_t n, const int64_t *colptr, const int64_t *rowval, const float *nzval, int64_t l,
+               int64_t u, float *A, int64_t lda, unsigned long long *dropped, bm_stream_t stream);
+
+/* Row-major band data to column-major band storage (the BandedRows copy of
+ * _BandedMatrix(::BandedRows, A), src/banded/BandedMatrix.jl:267-284): R is m x (l+u+1)
+ * column-major (ldr >= m) with A(i, c) at R[i + (c - i + l) * ldr]; the in-matrix slots
+ * of A ((l+u+1) x n, lda) are written. */
+int bm_dgbrows2cols(int64_t m, int64_t n, int64_t l, int64_t u, const double *R, int64_t ldr, double *A, int64_t lda,
+                    bm_stream_t stream);
+int bm_sgbrows2cols(int64_t m, int64_t n, int64_t l, int64_t u, const float *R, int64_t ldr, float *A, int64_t lda,
+                    bm_stream_t stream);
+
 /* ------------------------------------------------------------------ adjoint
  * Reverse-mode derivative of X = A \ B for an upstream gradient W = dL/dX (all
  * n x nrhs, leading dim n), with A's xGBTRF factors (LU, ldab, ipiv):
