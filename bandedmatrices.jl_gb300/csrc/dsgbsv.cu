@@ -13,6 +13,7 @@
 //                    x += FP64(LU32 \ FP32(r))
 // The host enqueues every launch up front; a device flag set by the check kernel
 // turns the remaining launches into no-ops, so the call never synchronises.
+#include "bandsolve.cuh"
 #include "mixedlu.cuh"
 #include "tclu.cuh"
 
@@ -161,51 +162,50 @@ __global__ void ds_check_kernel(i64 n, i64 nrhs, int k, int maxit, double tol, c
     R32[e] = (float)R[e];
 }
 
-// gbtrs 'N' with the FP32 factors, one warp per right-hand side of R32 (leading dim n).
-constexpr int kDsSolveStride = 10 * 32;  // 9 slots + the diagonal
-constexpr int kDsSolveWarps = 4;
-constexpr int kDsSolveSmem = kDsSolveWarps * (kSolveD + 1) * kDsSolveStride * 4;
-
-__device__ void ds_fwd(int ns, i64 n, int kl, int ku, const float* F, i64 ldf, const i64* ipiv, float* b, float* ring,
-                       int lane) {
-  switch (ns) {
-    case 1: blk_fwd_warp<1, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 2: blk_fwd_warp<2, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 3: blk_fwd_warp<3, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 4: blk_fwd_warp<4, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 5: blk_fwd_warp<5, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 6: blk_fwd_warp<6, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 7: blk_fwd_warp<7, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    case 8: blk_fwd_warp<8, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-    default: blk_fwd_warp<9, 1, kDsSolveStride>(n, kl, ku, 1, F, ldf, ipiv, b, n, ring, lane); break;
-  }
-}
-__device__ void ds_bwd(int ns, i64 n, int kv, const float* F, i64 ldf, float* b, float* ring, int lane) {
-  switch (ns) {
-    case 1: blk_bwd_warp<1, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 2: blk_bwd_warp<2, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 3: blk_bwd_warp<3, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 4: blk_bwd_warp<4, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 5: blk_bwd_warp<5, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 6: blk_bwd_warp<6, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 7: blk_bwd_warp<7, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    case 8: blk_bwd_warp<8, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-    default: blk_bwd_warp<9, 1, kDsSolveStride>(n, kv, 1, F, ldf, b, n, ring, lane); break;
-  }
+// gbtrs 'N' with the FP32 factors (ldf a multiple of 4): one warp per right-hand side
+// of R32 (leading dim n), the sweeps of bandsolve.cuh.
+template <int NSF, int NSB>
+__device__ void ds_sweeps(i64 n, int kl, int ku, const float* F, i64 ldf, const i64* ipiv, float* b, float* ring,
+                          uint64_t* bars, int* status) {
+  if (bs_sweep<NSF, true>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status))
+    bs_sweep<NSB, false>(n, kl, ku, F, ldf, ipiv, b, ring, bars + kBsStages, status);
 }
 
-__global__ void __launch_bounds__(32 * kDsSolveWarps) ds_solve_kernel(i64 n, int kl, int ku, i64 nrhs, const float* F,
-                                                                      i64 ldf, const i64* ipiv, float* R32,
-                                                                      const unsigned long long* W) {
+__global__ void __launch_bounds__(32) ds_solve_kernel(i64 n, int kl, int ku, i64 nrhs, const float* F, i64 ldf,
+                                                      const i64* ipiv, float* R32, const unsigned long long* W,
+                                                      int* status) {
   if (*reinterpret_cast<volatile const int*>(W + 1)) return;
-  extern __shared__ __align__(16) float ring_all[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const i64 c = (i64)blockIdx.x * kDsSolveWarps + w;
-  if (c >= nrhs) return;
-  float* ring = ring_all + w * (kSolveD + 1) * kDsSolveStride;
-  float* b = R32 + c * n;
-  ds_fwd(blk_ns(kl), n, kl, ku, F, ldf, ipiv, b, ring, lane);
-  ds_bwd(blk_ns(kl + ku), n, kl + ku, F, ldf, b, ring, lane);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);  // forward stages, then backward stages
+  float* ring = reinterpret_cast<float*>(smem_raw + 128);
+  const int lane = threadIdx.x & 31;
+  for (i64 c = blockIdx.x; c < nrhs; c += gridDim.x) {
+    if (lane == 0) {
+      for (int q = 0; q < 2 * kBsStages; ++q) mbar_init(&bars[q], 1);
+      fence_mbar_init();
+    }
+    __syncwarp();
+    float* b = R32 + c * n;
+    const int nf = bs_ns(kl), nb = bs_ns(kl + ku);
+    // forward window slots 2..8 (kl <= 224), backward 3..9 (64 <= kl+ku <= 256); narrower
+    // bands take the smallest instantiation that covers them
+    switch (nf <= 3 ? 3 : nf <= 5 ? 5 : 8) {
+      case 3:
+        if (nb <= 5) ds_sweeps<3, 5>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
+        else ds_sweeps<3, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
+        break;
+      case 5:
+        if (nb <= 7) ds_sweeps<5, 7>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
+        else ds_sweeps<5, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
+        break;
+      default: ds_sweeps<8, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status); break;
+    }
+    __syncwarp();
+    if (lane == 0)
+      for (int q = 0; q < 2 * kBsStages; ++q)
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[q])) : "memory");
+    __syncwarp();
+  }
 }
 
 int sgbtrf_tc_run(i64 n, i64 kl, i64 ku, const double* A, i64 lda, float* F, i64 ldf, i64* ipiv, i64* info,
@@ -234,6 +234,7 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
   if (ldx < std::max<i64>(1, n)) return -10;
   if (!ipiv && n > 0) return -11;
   if (!swork && n > 0) return -12;
+  if (reinterpret_cast<uintptr_t>(swork) & 15) return BM_ERR_ALIGN;
   if (!work && n * nrhs > 0) return -13;
   if (!(tol >= 0.0)) return -14;
   if (maxit < 0) return -15;
@@ -251,7 +252,7 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
   if ((r = cuda_status(cudaMemsetAsync(berr, 0, sizeof(double), s), name))) return r;
   if (n == 0 || nrhs == 0) {
     if (n > 0) {  // factor only
-      const i64 ldf = 2 * kl + ku + 1;
+      const i64 ldf = (2 * kl + ku + 1 + 3) & ~(i64)3;
       if (tc_lu_fits(kl, ku)) return sgbtrf_tc_run(n, kl, ku, AB, ldab, swork, ldf, ipiv, info, s, name);
       const int blocks = (int)std::min<i64>(ceil_div(ldf * n, 256), (i64)num_sms() * 8);
       ds_round_kernel<<<blocks, 256, 0, s>>>(n, (int)kl, (int)ku, AB, ldab, swork, ldf);
@@ -260,7 +261,7 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
     }
     return BM_OK;
   }
-  const i64 ldf = 2 * kl + ku + 1;
+  const i64 ldf = (2 * kl + ku + 1 + 3) & ~(i64)3;  // a multiple of 4: 16-byte column segments
   float* F = swork;
   float* R32 = swork + ldf * n;
   double* R = work;
@@ -285,11 +286,12 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
   ds_after_factor_kernel<<<1, 1, 0, s>>>(info, W, iter, berr);
   if ((r = launch_status(name))) return r;
   // ---- first solve
-  if ((r = cuda_status(ensure_smem((const void*)ds_solve_kernel, kDsSolveSmem), name))) return r;
-  const int sblocks = (int)ceil_div(nrhs, (i64)kDsSolveWarps);
+  const int ssmem = bs_smem_bytes((int)kl, (int)ku);
+  if ((r = cuda_status(ensure_smem((const void*)ds_solve_kernel, ssmem), name))) return r;
+  const int sblocks = (int)std::min<i64>(nrhs, (i64)nsm * 4);
   ds_b_to_r32_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, B, ldb, R32, W);
   if ((r = launch_status(name))) return r;
-  ds_solve_kernel<<<sblocks, 32 * kDsSolveWarps, kDsSolveSmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W);
+  ds_solve_kernel<<<sblocks, 32, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
   if ((r = launch_status(name))) return r;
   ds_update_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, R32, X, ldx, 1, W);
   if ((r = launch_status(name))) return r;
@@ -305,8 +307,7 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
     ds_check_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, k, mx, tol, R, R32, W, iter, berr);
     if ((r = launch_status(name))) return r;
     if (k == mx) break;
-    ds_solve_kernel<<<sblocks, 32 * kDsSolveWarps, kDsSolveSmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32,
-                                                                      W);
+    ds_solve_kernel<<<sblocks, 32, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
     if ((r = launch_status(name))) return r;
     ds_update_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, R32, X, ldx, 0, W);
     if ((r = launch_status(name))) return r;

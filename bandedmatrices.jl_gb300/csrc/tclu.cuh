@@ -17,11 +17,14 @@
 //   Per panel:
 //     1. wait for panel k-1's MMAs;
 //     2. the panel quarter's warp copies its 32 columns (rows j0 .. j0+klr-1) from
-//        TMEM to the shared-memory panel P; rows j0+klr .. j0+R-1 enter from the FP64
-//        band (rounded to FP32): into P for the panel columns, into TMEM for the
-//        trailing quarters; the columns j0+kvr .. j0+kvr+31 enter the free quarter,
-//        every window row (zero outside the band);
-//     3. partial-pivot LU of the R x 32 panel, one row per thread: the pivot is the
+//        TMEM to the shared-memory panel P; rows j0+klr .. j0+R-1 enter from the
+//        staging buffer (FP64 band values rounded to FP32, loaded during the previous
+//        panel): into P for the panel columns, into TMEM for the trailing quarters; the
+//        columns j0+kvr .. j0+kvr+31 enter the free quarter, every window row (zero
+//        outside the band);
+//     3. partial-pivot LU of the R x 32 panel by the R/32 warps that hold a row each
+//        (a named barrier among them), while the other warps load the next panel's
+//        entering rows and columns into the staging buffer: the pivot is the
 //        largest |a| (exact to 2^-15 relative; the first row among near-equals), the
 //        interchange covers the step's columns onward, scaling by the rounded
 //        reciprocal, rank-1 update of the later panel columns;
@@ -32,7 +35,8 @@
 //        to nearest) as the B operand;
 //     6. each trailing quarter's warp applies the panel's interchanges to its TMEM
 //        rows, solves U12 = L11^-1 A12 for its 32 columns (rows j0 .. j0+31, in
-//        registers), stores U12 to the factor storage and writes it, split, as the A
+//        registers), stores U12 to the factor storage (column by column through the
+//        warp's shared tile, so the stores coalesced) and writes it, split, as the A
 //        operand (M = band columns, K = panel columns);
 //     7. one thread issues, per TMEM region, D[cols, rows j0+32 ..] -= A B as three
 //        kind::tf32 MMAs per K = 8 step (hi*hi + hi*lo + lo*hi: FP32-level products)
@@ -59,7 +63,10 @@ __host__ __device__ inline int tc_off_P() { return kTcHdr; }
 __host__ __device__ inline int tc_off_A(int kl) { return kTcHdr + ((kTcNB * tc_rs(kl) * 4 + 1023) / 1024) * 1024; }
 __host__ __device__ inline int tc_off_B(int kl) { return tc_off_A(kl) + 4 * 16384; }
 __host__ __device__ inline int tc_off_T(int kl) { return tc_off_B(kl) + 2 * tc_klr(kl) * kTcNB * 4; }
-__host__ __device__ inline int tc_smem_bytes(int kl) { return tc_off_T(kl) + 8 * 32 * 32 * 4; }
+// staging of the rows and columns the next panel brings in, FP32: [256 columns][32 rows]
+// and [32 columns][64 rows], both XOR-swizzled on the row (conflict-free by row and by column)
+__host__ __device__ inline int tc_off_S(int kl) { return tc_off_T(kl) + 8 * 32 * 32 * 4; }
+__host__ __device__ inline int tc_smem_bytes(int kl) { return tc_off_S(kl) + (256 * 32 + 32 * 64) * 4; }
 
 __host__ __device__ inline bool tc_lu_fits(long long kl, long long ku) {
   return kl >= 1 && ku >= 0 && kl + ku >= 64 && kl + ku <= 256 && kl <= 224;
@@ -88,7 +95,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   float* Bhi = reinterpret_cast<float*>(smem + tc_off_B(kl));  // [klr x 32] operand layout
   float* Blo = Bhi + klr * kTcNB;
   float* Tw = reinterpret_cast<float*>(smem + tc_off_T(kl)) + warp * 1024;  // [32 rows][32 lanes]
+  float* Srow = reinterpret_cast<float*>(smem + tc_off_S(kl));  // new rows: column cr, row r at cr*32 + (r ^ (cr & 31))
+  float* Scol = Srow + 256 * 32;                                 // new columns: q, row r at q*64 + (r ^ q)
+  const int nw_lu = R / 32;  // warps of the panel factorization; the others stage the next panel
 
+  // barrier of the panel-factorization warps only
+  auto lu_sync = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(32 * nw_lu) : "memory"); };
   auto aval = [&](i64 i, i64 c) -> float {
     const i64 d = i - c;
     return (i < n && c < n && d <= kl && d >= -ku) ? (float)A[(ku + d) + c * lda] : 0.0f;
@@ -119,6 +131,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     tc::wait_st();
   }
+  // The rows and columns panel (j1 / 32) brings in, from the FP64 band, rounded to FP32:
+  // rows j1+klr .. j1+klr+31 over its columns j1 .. j1+kvr-1, and the window's last 64
+  // rows over the 32 columns j1+kvr .. (the rows above are zero: outside the band).
+  // Threads lt = 0 .. nt-1 of the caller; eight loads in flight per thread.
+  auto stage = [&](i64 j1, int lt, int nt) {
+    const int tot_r = kvr * 32, tot = tot_r + 32 * 64;
+    for (int e0 = lt; e0 < tot; e0 += 8 * nt) {
+      float v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * nt;
+        v[q] = 0.0f;
+        if (e < tot_r) v[q] = aval(j1 + klr + (e & 31), j1 + (e >> 5));
+        else if (e < tot) {
+          const int f = e - tot_r;
+          v[q] = aval(j1 + klr - 32 + (f & 63), j1 + kvr + (f >> 6));
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int e = e0 + q * nt;
+        if (e < tot_r) Srow[(e >> 5) * 32 + ((e & 31) ^ ((e >> 5) & 31))] = v[q];
+        else if (e < tot) {
+          const int f = e - tot_r;
+          Scol[(f >> 6) * 64 + ((f & 63) ^ (f >> 6))] = v[q];
+        }
+      }
+    }
+  };
+  stage(0, tid, kTcThreads);
+  __syncthreads();
   long long inf = 0;  // thread 0
   i64 k = 0;
   for (i64 j0 = 0; j0 < n; j0 += kTcNB, ++k) {
@@ -148,27 +191,29 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                                                                __uint_as_float(v[4 * q + 3]));
       }
     }
-    for (int e = tid; e < 32 * 32; e += kTcThreads) {  // new rows, panel columns
+    for (int e = tid; e < 32 * 32; e += kTcThreads) {  // new rows, panel columns (staged)
       const int c = e >> 5, r = e & 31;
-      P[c * RS + klr + r] = aval(j0 + klr + r, j0 + c);
+      P[c * RS + klr + r] = Srow[c * 32 + (r ^ c)];
     }
     {
       const int rel = (warp - wp + 8) & 7;
       const int relt = rel == 0 ? 8 : rel;  // position after the panel quarter: 1 .. 8
       if (relt == nq) {                     // new columns j0 + kvr + lane: every window row
-        const i64 c = j0 + kvr + lane;
-        for (int m = 0; m < R / 32; ++m) {
-          uint32_t v[32];
-#pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = __float_as_uint(aval(j0 + 32 * m + i, c));
-          tc::st32(taddr(warp, (int)((j0 + 32 * m) & 255)), v);
-        }
-        tc::wait_st();
-      } else if (relt < nq) {  // trailing quarter: the new rows
-        const i64 c = j0 + 32 * relt + lane;
         uint32_t v[32];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = __float_as_uint(aval(j0 + klr + i, c));
+        for (int i = 0; i < 32; ++i) v[i] = 0u;  // rows above the band
+        for (int m = 0; m < R / 32 - 2; ++m) tc::st32(taddr(warp, (int)((j0 + 32 * m) & 255)), v);
+        for (int m = 0; m < 2; ++m) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] = __float_as_uint(Scol[lane * 64 + ((32 * m + i) ^ lane)]);
+          tc::st32(taddr(warp, (int)((j0 + klr - 32 + 32 * m) & 255)), v);
+        }
+        tc::wait_st();
+      } else if (relt < nq) {  // trailing quarter: the new rows (staged)
+        const int cr = 32 * relt + lane;
+        uint32_t v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = __float_as_uint(Srow[cr * 32 + (i ^ lane)]);
         tc::st32(taddr(warp, (int)((j0 + klr) & 255)), v);
         tc::wait_st();
       }
@@ -177,8 +222,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc::fence_after();
 
-    // ---- 3. panel LU, thread t = window row t
-    {
+    // ---- 3. panel LU, thread t = window row t, by the nw_lu warps (named barrier 1);
+    // meanwhile the other warps stage the next panel's rows and columns
+    if (warp >= nw_lu) {
+      stage(j0 + kTcNB, tid - 32 * nw_lu, kTcThreads - 32 * nw_lu);
+    } else {
       float a[kTcNB];
       const bool has_row = tid < R;
 #pragma unroll
@@ -196,10 +244,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           key = __reduce_max_sync(0xffffffffu, key);
           if (lane == 0) wkey[par * 8 + warp] = key;
-          __syncthreads();
+          lu_sync();
           uint32_t best = wkey[par * 8];
-#pragma unroll
-          for (int w2 = 1; w2 < 8; ++w2) best = max(best, wkey[par * 8 + w2]);
+          for (int w2 = 1; w2 < nw_lu; ++w2) best = max(best, wkey[par * 8 + w2]);
           const int p = 255 - (int)(best & 255u);
           float* pr = prow + 32 * par;
           float* cr = crow + 32 * par;
@@ -211,7 +258,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (int c2 = c; c2 < kTcNB; ++c2) cr[c2] = a[c2];
           }
-          __syncthreads();
+          lu_sync();
           const float pv = pr[c];
           const bool nz = is_nonzero(pv);
           if (tid == 0) {
@@ -246,6 +293,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
     }
     __syncthreads();
+    if (nw_lu == 8) {  // no spare warp: stage the next panel now
+      stage(j0 + kTcNB, tid, kTcThreads);
+      __syncthreads();
+    }
     // ---- 4. panel columns to the factor storage (dgbtf2's layout), then the later
     // interchanges on the L columns
     for (int e = tid; e < kTcNB * R; e += kTcThreads) {
@@ -319,12 +370,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
           for (int i = kk + 1; i < 32; ++i) u[i] = fmaf(-lk[i], u[kk], u[i]);
         }
-        if (c < n) {
+        // U12 to the factor storage, a column per pass of the warp (lane = row)
+        __syncwarp();
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const i64 d = (j0 + i) - c;  // U(j0+i, c): -kv <= d < 0
-            if (i < jb && d >= -kv) F[(kv + d) + c * ldf] = u[i];
-          }
+        for (int i = 0; i < 32; ++i) Tw[i * 32 + (lane ^ i)] = u[i];  // row i, column lane (swizzled)
+        __syncwarp();
+        for (int q = 0; q < 32; ++q) {
+          const i64 cq = j0 + 32 * relt + q, d = (j0 + lane) - cq;  // U(j0+lane, cq): -kv <= d < 0
+          if (cq < n && lane < jb && d >= -kv) F[(kv + d) + cq * ldf] = Tw[lane * 32 + (q ^ lane)];
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {

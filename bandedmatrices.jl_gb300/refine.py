@@ -41,7 +41,8 @@ def solve_refined(A: BandedMatrix, b: torch.Tensor, tol: float = 1e-10, maxit: i
     dev = A.device
     X = torch.empty(nrhs, n, dtype=torch.float64, device=dev).t()
     ipiv = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
-    swork = torch.empty((2 * kl + ku + 1) * n + n * nrhs + 1, dtype=torch.float32, device=dev)
+    ldf = (2 * kl + ku + 1 + 3) // 4 * 4
+    swork = torch.empty(ldf * n + n * nrhs + 1, dtype=torch.float32, device=dev)
     work = torch.empty(n * nrhs + 3 * nrhs + 2, dtype=torch.float64, device=dev)
     it = torch.empty(1, dtype=torch.int32, device=dev)
     berr = torch.empty(1, dtype=torch.float64, device=dev)

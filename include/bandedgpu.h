@@ -389,7 +389,8 @@ int bm_dsgbsv_batched_sched(int64_t count, const bm_gb_desc *descs, const int32_
  * the FP32 factorization's pivots, *info (device) its info (> 0: exactly singular in
  * FP32; nothing is solved and *berr is +inf), *iter (device int32) the corrections
  * taken, *berr (device double) the final backward error.  Workspace: swork, FP32,
- * (2kl+ku+1)*n + n*nrhs floats (the factors in gbtrf layout, then the correction);
+ * 16-byte aligned, ldf*n + n*nrhs floats with ldf = 2kl+ku+1 rounded up to a multiple
+ * of 4 (the factors in gbtrf layout with leading dimension ldf, then the correction);
  * work, FP64, n*nrhs + 3*nrhs + 2 doubles.  kl + ku <= 256.  The whole loop is
  * enqueued at once and decided on the device (a flag turns the remaining launches
  * into no-ops): no host synchronisation, no allocation.  No counterpart in the
