@@ -68,6 +68,11 @@ SIGNATURES: dict[str, list] = {
     "bm_sgbshift": [i64, i64, i64, i64, F, P, i64, P],
     "bm_dgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
     "bm_sgbdot": [i64, i64, i64, i64, P, P, i64, P, P, P, P],
+    "bm_plan_create": [P, i64, P, P, I, P, P, P],
+    "bm_plan_destroy": [P],
+    "bm_plan_schedule": [P, P, P, P],
+    "bm_plan_execute_dgbsv": [P, P, P, P, P, P, P],
+    "bm_plan_execute_dsgbsv": [P, P, P, P, P, P, P, P, P, P, P, D, i64, P],
     "bm_gb2csc_nnz": [i64, i64, i64, i64],
     "bm_dgb2csc": [i64, i64, i64, i64, P, i64, P, P, P, P],
     "bm_sgb2csc": [i64, i64, i64, i64, P, i64, P, P, P, P],

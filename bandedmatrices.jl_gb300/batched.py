@@ -212,9 +212,56 @@ class BandedBatch:
         n, k, off = int(self.n[s]), int(self.nrhs[s]), int(self.b_off[s])
         return self.X[off: off + n * k].view(k, n).t()
 
+    def make_plan(self, mode: str = "plain") -> "Plan":
+        """A library-owned plan (bm_plan_create): the autotuned schedule of this batch for the
+        plain ("plain") or refined ("mixed") solve, timed on a copy of the batch."""
+        return Plan(self, mode)
+
     def capture(self) -> torch.cuda.CUDAGraph:
         """Capture factor_solve in a CUDA graph (call once eagerly first for device set-up)."""
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self.factor_solve()
         return g
+
+
+class Plan:
+    """bm_plan: the batch's autotuned schedule and its device workspace, owned by the
+    library (the C-ABI counterpart of BandedBatch.tune).  Release with close()."""
+
+    def __init__(self, batch: BandedBatch, mode: str = "plain"):
+        if mode not in ("plain", "mixed") or batch.dtype != torch.float64:
+            raise ValueError("plans cover the Float64 plain and refined batched solves")
+        self.batch, self.mode = batch, mode
+        self.handle = ctypes.c_void_p()
+        host = np.ascontiguousarray(batch.descs.cpu().numpy())
+        _lib.call("bm_plan_create", ctypes.byref(self.handle), batch.count, ctypes.c_void_p(host.ctypes.data),
+                  _ptr(batch.descs), 0 if mode == "plain" else 1, _ptr(batch.AB), _ptr(batch.B), _stream(batch.device))
+        sched, ms, cand = Schedule(), ctypes.c_double(), ctypes.c_int64()
+        _lib.call("bm_plan_schedule", self.handle, ctypes.byref(sched), ctypes.byref(ms), ctypes.byref(cand))
+        self.schedule, self.tuned_ms, self.candidates = sched, ms.value, cand.value
+
+    def execute(self, tol: float = 1e-10, maxit: int = 30, stream=None) -> None:
+        """The scheduled solve of the plan's batch (factor_solve / solve_mixed semantics)."""
+        b = self.batch
+        st = ctypes.c_void_p(stream) if stream is not None else _stream(b.device)
+        if self.mode == "plain":
+            _lib.call("bm_plan_execute_dgbsv", self.handle, _ptr(b.descs), _ptr(b.AB), _ptr(b.ipiv), _ptr(b.B),
+                      _ptr(b.info), st)
+            return
+        if not hasattr(b, "X"):
+            b.solve_mixed(tol, maxit)  # allocates the refined solve's buffers once
+        _lib.call("bm_plan_execute_dsgbsv", self.handle, _ptr(b.descs), _ptr(b.AB), _ptr(b.B), _ptr(b.X),
+                  _ptr(b.ipiv), _ptr(b.info), _ptr(b.AB32), _ptr(b.R32), _ptr(b.iters), _ptr(b.berr),
+                  ctypes.c_double(tol), int(maxit), st)
+
+    def close(self) -> None:
+        if self.handle:
+            _lib.call("bm_plan_destroy", self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

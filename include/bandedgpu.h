@@ -409,6 +409,31 @@ int bm_dsgbsv(int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double *AB,
 int bm_sgbtrf_tc(int64_t n, int64_t kl, int64_t ku, const double *AB, int64_t ldab, float *F, int64_t ldf,
                  int64_t *ipiv, int64_t *info, bm_stream_t stream);
 
+/* Plans: the autotuned schedule of a batch and its device workspace, owned by the
+ * library.  bm_plan_create times every candidate bm_gb_schedule (4 or 8 warps per CTA x
+ * the wide/narrow split at 0, 8, 16, 24, 32, 48, 64, 96 or all band columns) on a copy
+ * of the batch (AB, B: device buffers laid out by the descriptors; not modified) for the
+ * plain FP64 solve (kind 0) or the refined solve (kind 1), keeps the fastest, and
+ * stores its processing order and work counters in device memory it allocates; the
+ * choice is cached per (device, batch shape) for the process.  host_descs is a host copy
+ * of the count descriptors in descs (device).  It allocates and synchronises: call it
+ * once, outside any stream capture.  The executions enqueue the scheduled solve with
+ * no allocation and no synchronisation.  No counterpart in the reference (which
+ * solves one system per call). */
+typedef struct bm_plan_st *bm_plan;
+int bm_plan_create(bm_plan *plan, int64_t count, const bm_gb_desc *host_descs, const bm_gb_desc *descs, int kind,
+                   const double *AB, const double *B, bm_stream_t stream);
+int bm_plan_destroy(bm_plan plan);
+/* The plan's schedule, the time of its timing run (ms) and the candidates timed. */
+int bm_plan_schedule(bm_plan plan, bm_gb_schedule *sched, double *tuned_ms, int64_t *candidates);
+/* bm_dgbsv_batched_sched with the plan's schedule (kind 0). */
+int bm_plan_execute_dgbsv(bm_plan plan, const bm_gb_desc *descs, double *AB, int64_t *ipiv, double *B, int64_t *info,
+                          bm_stream_t stream);
+/* bm_dsgbsv_batched_sched with the plan's schedule (kind 1). */
+int bm_plan_execute_dsgbsv(bm_plan plan, const bm_gb_desc *descs, const double *AB, const double *B, double *X,
+                           int64_t *ipiv, int64_t *info, float *AB32, float *R32, int32_t *iters, double *berr,
+                           double tol, int64_t maxit, bm_stream_t stream);
+
 /* Allocation-free variant of bm_dgbsv_batched, for callers that cannot allocate
  * device memory when they solve: real-time loops that must not block on an
  * allocator, and hosts whose device memory belongs to another runtime's pool (Julia's

@@ -373,3 +373,49 @@ def test_wide_band_panels_bitexact(bm, gpu, orc, dt, m, n, l, u, zero_cols):
             assert np.array_equal(F.solve(bd).cpu().numpy(), orc.gbtrs("N", n, l, u, LU, ipiv, b))
             assert rel(F.T.solve(bd).cpu().numpy(), orc.gbtrs("T", n, l, u, LU, ipiv, b)) < \
                 (1e-12 if dt == np.float64 else 1e-5)
+
+
+def test_plan_matches_the_regular_batched_solve(bm, gpu):
+    """bm_plan_create / bm_plan_execute_* (the library-owned autotuner) give, per system,
+    exactly what the regular batched entry points give, for the plain and the refined
+    solve; the plan's schedule is one of the timed candidates and is reused from the
+    process cache for a batch of the same shape."""
+    rng = np.random.default_rng(77)
+    count = 200
+    n = np.exp(rng.uniform(np.log(64), np.log(3000), count)).astype(np.int64)
+    kl = rng.integers(1, 41, count)
+    ku = rng.integers(1, 41, count)
+    nrhs = rng.integers(1, 4, count)
+    batch = bm.BandedBatch(n, kl, ku, nrhs, torch.float64, gpu)
+    g = torch.Generator(device=gpu)
+    g.manual_seed(3)
+    for s in range(count):
+        mb = batch.matrix_band(s)
+        mb.normal_(generator=g)
+        mb[int(ku[s])] += 2.0 * (kl[s] + ku[s])
+        batch.rhs(s).normal_(generator=g)
+    AB0, B0 = batch.AB.clone(), batch.B.clone()
+    batch.factor_solve()
+    torch.cuda.synchronize()
+    ref_B, ref_ipiv = batch.B.clone(), batch.ipiv.clone()
+    batch.AB.copy_(AB0)
+    batch.B.copy_(B0)
+    plan = batch.make_plan("plain")
+    assert plan.candidates >= 2 and plan.tuned_ms > 0
+    assert torch.equal(batch.AB, AB0) and torch.equal(batch.B, B0)  # timing ran on a copy
+    plan.execute()
+    torch.cuda.synchronize()
+    assert torch.equal(batch.B, ref_B) and torch.equal(batch.ipiv, ref_ipiv)
+    batch.AB.copy_(AB0)
+    batch.B.copy_(B0)
+    again = batch.make_plan("plain")  # same shape: the cached choice
+    assert (again.schedule.n_wide, again.schedule.warps) == (plan.schedule.n_wide, plan.schedule.warps)
+    again.close()
+    plan.close()
+    X_ref = batch.solve_mixed(1e-12, 20).clone()
+    mp = batch.make_plan("mixed")
+    batch.X.zero_()
+    mp.execute(1e-12, 20)
+    torch.cuda.synchronize()
+    assert torch.equal(batch.X, X_ref)
+    mp.close()
