@@ -62,8 +62,13 @@ static int gb_adjoint_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const T* lu, i64 lda
   if (kl < 0) return -2;
   if (ku < 0) return -3;
   if (nrhs < 0) return -4;
+  const bool work = n > 0 && nrhs > 0;  // the pointers are read only when there is work
+  if (!lu && work) return -5;
   if (ldab < 2 * kl + ku + 1) return -6;
-  if (!X && (!B || !Xwork)) return -8;
+  if (!ipiv && work) return -7;
+  if (!X && (!B || !Xwork) && work) return -8;
+  if (!W && work) return -10;
+  if (!gB && work) return -11;
   if (ldg < kl + ku + 1) return -13;
   if (n == 0 || nrhs == 0) return BM_OK;
   const size_t bytes = sizeof(T) * (size_t)n * (size_t)nrhs;

@@ -288,8 +288,9 @@ int bm_sgbrows2cols(int64_t m, int64_t n, int64_t l, int64_t u, const float *R, 
  *   grad_B    <- A^{-T} W                      (transposed xGBTRS on the factors)
  *   grad_band <- -(A^{-T} W) X^T on A's band   (BLAS band layout, (kl+ku+1) x n,
  *                                               leading dim ldg; NULL to skip)
- * X may be NULL: it is then recomputed from B into Xwork (n x nrhs workspace).  No
- * counterpart in the reference; it is the rrule of \ built on the transposed solve
+ * X may be NULL: it is then recomputed from B into Xwork (n x nrhs workspace).  LU,
+ * ipiv, W and grad_B are read or written only when n > 0 and nrhs > 0, and must then
+ * be non-NULL (-5, -7, -10, -11).  No counterpart in the reference; it is the rrule of \ built on the transposed solve
  * ldiv!(transpose(F), B) (src/banded/linalg.jl:41-47). */
 int bm_dgbsv_adjoint(int64_t n, int64_t kl, int64_t ku, int64_t nrhs, const double *LU, int64_t ldab,
                      const int64_t *ipiv, const double *X, const double *B, const double *W, double *grad_B,

@@ -164,10 +164,17 @@ def test_product_qr_triangular_and_adjoint_codes_without_gpu(bm):
     assert L.bm_dtbsv(b"U", b"N", b"N", 8, 2, f, 2, f, 1, s) == -7
     assert L.bm_dtbsv(b"U", b"T", b"N", 8, 2, f, 3, f, 0, s) == -9
     # adjoint(n, kl, ku, nrhs, LU, ldab, ipiv, X, B, W, grad_B, grad_band, ldg, Xwork, stream)
-    adj = lambda n=8, nrhs=1, ldab=6, X=f, B=f, ldg=4, Xw=f: L.bm_dgbsv_adjoint(
-        n, 2, 1, nrhs, f, ldab, f, X, B, f, f, f, ldg, Xw, s)
+    adj = lambda n=8, nrhs=1, LU=f, ldab=6, ip=f, X=f, B=f, W=f, gB=f, ldg=4, Xw=f: L.bm_dgbsv_adjoint(
+        n, 2, 1, nrhs, LU, ldab, ip, X, B, W, gB, f, ldg, Xw, s)
     assert adj(n=-1) == -1
     assert adj(nrhs=-1) == -4
+    assert adj(LU=None) == -5
     assert adj(ldab=5) == -6
+    assert adj(ip=None) == -7
     assert adj(X=None, Xw=None) == -8  # X not kept and no workspace to recompute it in
+    assert adj(W=None) == -10
+    assert adj(gB=None) == -11
     assert adj(ldg=3) == -13
+    # nothing to do: the data pointers are not read (an empty call succeeds without a GPU)
+    assert adj(n=0, LU=None, ip=None, W=None, gB=None) == 0
+    assert adj(nrhs=0, LU=None, ip=None, W=None, gB=None) == 0
