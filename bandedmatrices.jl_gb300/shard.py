@@ -82,6 +82,34 @@ def exchange_halo(x_local: torch.Tensor, r0: int, r1: int, n: int, l: int, u: in
     return out
 
 
+def gbmv_rows(data_block: torch.Tensor, n: int, l: int, u: int, x_local: torch.Tensor, world: int, rank: int,
+              group=None, alpha: float = 1.0, out: torch.Tensor | None = None) -> torch.Tensor:
+    """This rank's rows [r0, r1) (``row_ranges(n, world)[rank]``) of y = alpha A x for a
+    square n x n (l, u) band, with x distributed in the same row blocks.
+
+    ``data_block`` is the rank's slice of the band storage: columns [c0, c1) of
+    ``row_block`` (all l+u+1 storage rows, column-major, on this rank's GPU).  The
+    x-halo arrives by ``exchange_halo`` (x_local on the device for NCCL, on the host for
+    gloo: it is moved to the band's device afterwards); the rows are then one call of
+    the library's gbmv on the block read as an (r1-r0) x (c1-c0) band with bandwidths
+    (l - d, u + d), d = r0 - c0 -- no further exchange.  Each output row keeps the
+    unsharded accumulation order, so the gathered result equals A*x bit for bit."""
+    from .banded import BandedMatrix, gbmv
+
+    r0, r1 = row_ranges(n, world)[rank]
+    blk = row_block(n, n, l, u, r0, r1)
+    if data_block.shape != (l + u + 1, blk["n"]):
+        raise ValueError(f"data_block must be the {l + u + 1} x {blk['n']} storage columns [{blk['c0']}, {blk['c1']})")
+    if x_local.shape != (r1 - r0,):
+        raise ValueError(f"x_local must hold the {r1 - r0} entries of rows [{r0}, {r1})")
+    halo = exchange_halo(x_local, r0, r1, n, l, u, world, rank, group).to(data_block.device)
+    y = out if out is not None else torch.empty(r1 - r0, dtype=data_block.dtype, device=data_block.device)
+    if blk["m"] == 0:
+        return y
+    gbmv("N", alpha, BandedMatrix(data_block, blk["m"], blk["l"], blk["u"]), halo, 0.0, y)
+    return y
+
+
 def batch_shards(n, kl, ku, nrhs, world: int) -> list[np.ndarray]:
     """System indices per rank: longest first onto the least-loaded rank."""
     n, kl, ku, nrhs = (np.asarray(v, dtype=np.int64) for v in (n, kl, ku, nrhs))

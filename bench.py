@@ -770,7 +770,7 @@ def run_pde(bm, dev, stream, G=512):
 def run_case(args):
     """One named workload, repeated --reps times (for profiler captures); prints the
     device time of each repetition.  Cases: gbmv_{f32,f64}_l{L}, gbmm_{f32,f64}_l{L},
-    batched_plain, batched_mixed, lu_single_l{L}, qr_l{L}."""
+    batched_plain, batched_mixed, lu_single_l{L}, refined_l{L}, qr_l{L}."""
     import numpy as np
     import torch
     import __graft_entry__ as ge
@@ -823,6 +823,14 @@ def run_case(args):
         A.data[lu] += 2.0 * lu + 1.0
         b = torch.randn(n, dtype=dt, device=dev, generator=g)
         fn = lambda: A.solve(b)
+    elif parts[0] == "refined":
+        # the single-system refined solve (randn + 16 I, b randn), as refined_single times it
+        n = args.n or (1 << 20)
+        A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, torch.float64, dev), n, lu, lu)
+        A.data.normal_(generator=g)
+        A.data[lu] += 16.0
+        b = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+        fn = lambda: bm.solve_refined(A, b, tol=1e-10)
     elif parts[0] == "qr":
         n = args.n or (1 << 18)
         A = bm.BandedMatrix(bm.band_storage(2 * lu + 1, n, dt, dev), n, lu, lu)
