@@ -36,8 +36,8 @@ int launch_status(const char* where);
 inline i64 ceil_div(i64 a, i64 b) { return (a + b - 1) / b; }
 
 // ---------------------------------------------------------------- device side
-// Spin limits.  Every wait in these kernels is bounded: on expiry the kernel
-// records BM_STATUS_TIMEOUT in the status word and stops waiting.
+// Spin limits.  Every wait in these kernels is bounded, in polls and in time: on
+// expiry the kernel records BM_STATUS_TIMEOUT in the status word and stops waiting.
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 enum : int { BM_STATUS_TIMEOUT = 1 };
@@ -93,12 +93,28 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// A poll of mbarrier.try_wait may suspend the thread for a hardware-chosen time, so a
+// poll count alone does not bound a wait's duration: every wait also gives up after
+// kWaitNs of global time.
+constexpr uint64_t kWaitNs = 2000000000ull;
+
 // Bounded wait for phase `phase` of `bar`: at most `limit` polls (never more than
-// kSpinLimit).  Returns false on timeout.
+// kSpinLimit) and at most kWaitNs.  Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit = kSpinLimit) {
   if (limit > kSpinLimit) limit = kSpinLimit;
-  for (uint32_t it = 0; it < limit; ++it)
+  if (mbar_try_wait(bar, phase)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 1; it < limit; ++it) {
     if (mbar_try_wait(bar, phase)) return true;
+    if ((it & 15) == 0 && global_ns() - t0 > kWaitNs) return false;
+  }
   return false;
 }
 

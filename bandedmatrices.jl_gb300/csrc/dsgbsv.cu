@@ -162,49 +162,31 @@ __global__ void ds_check_kernel(i64 n, i64 nrhs, int k, int maxit, double tol, c
     R32[e] = (float)R[e];
 }
 
-// gbtrs 'N' with the FP32 factors (ldf a multiple of 4): one warp per right-hand side
-// of R32 (leading dim n), the sweeps of bandsolve.cuh.
-template <int NSF, int NSB>
-__device__ void ds_sweeps(i64 n, int kl, int ku, const float* F, i64 ldf, const i64* ipiv, float* b, float* ring,
-                          uint64_t* bars, int* status) {
-  if (bs_sweep<NSF, true>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status))
-    bs_sweep<NSB, false>(n, kl, ku, F, ldf, ipiv, b, ring, bars + kBsStages, status);
-}
-
-__global__ void __launch_bounds__(32) ds_solve_kernel(i64 n, int kl, int ku, i64 nrhs, const float* F, i64 ldf,
-                                                      const i64* ipiv, float* R32, const unsigned long long* W,
-                                                      int* status) {
+// gbtrs 'N' with the FP32 factors (ldf a multiple of 4): one CTA of kBsWarps warps per
+// right-hand side of R32 (leading dim n), the sweeps of bandsolve.cuh.  A sweep whose
+// wait ran out ends the CTA (its copies landed): the status word reports it.
+__global__ void __launch_bounds__(32 * kBsWarps) ds_solve_kernel(i64 n, int kl, int ku, i64 nrhs, const float* F,
+                                                                 i64 ldf, const i64* ipiv, float* R32,
+                                                                 const unsigned long long* W, int* status) {
   if (*reinterpret_cast<volatile const int*>(W + 1)) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);  // forward stages, then backward stages
-  float* ring = reinterpret_cast<float*>(smem_raw + 128);
-  const int lane = threadIdx.x & 31;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);  // forward slots, then backward slots
+  const int stages = bs_stages(ldf);
   for (i64 c = blockIdx.x; c < nrhs; c += gridDim.x) {
-    if (lane == 0) {
-      for (int q = 0; q < 2 * kBsStages; ++q) mbar_init(&bars[q], 1);
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < 8; ++q) mbar_init(&bars[q], 1);
       fence_mbar_init();
     }
-    __syncwarp();
+    __syncthreads();
     float* b = R32 + c * n;
-    const int nf = bs_ns(kl), nb = bs_ns(kl + ku);
-    // forward window slots 2..8 (kl <= 224), backward 3..9 (64 <= kl+ku <= 256); narrower
-    // bands take the smallest instantiation that covers them
-    switch (nf <= 3 ? 3 : nf <= 5 ? 5 : 8) {
-      case 3:
-        if (nb <= 5) ds_sweeps<3, 5>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
-        else ds_sweeps<3, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
-        break;
-      case 5:
-        if (nb <= 7) ds_sweeps<5, 7>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
-        else ds_sweeps<5, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status);
-        break;
-      default: ds_sweeps<8, 9>(n, kl, ku, F, ldf, ipiv, b, ring, bars, status); break;
-    }
-    __syncwarp();
-    if (lane == 0)
-      for (int q = 0; q < 2 * kBsStages; ++q)
+    const bool ok = bs_sweep<true>(n, kl, ku, F, ldf, ipiv, b, smem_raw, bars, stages, status) &&
+                    bs_sweep<false>(n, kl, ku, F, ldf, ipiv, b, smem_raw, bars + 4, stages, status);
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int q = 0; q < 8; ++q)
         asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bars[q])) : "memory");
-    __syncwarp();
+    __syncthreads();
+    if (!ok) return;
   }
 }
 
@@ -286,12 +268,12 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
   ds_after_factor_kernel<<<1, 1, 0, s>>>(info, W, iter, berr);
   if ((r = launch_status(name))) return r;
   // ---- first solve
-  const int ssmem = bs_smem_bytes((int)kl, (int)ku);
+  const int ssmem = bs_smem_bytes(ldf);
   if ((r = cuda_status(ensure_smem((const void*)ds_solve_kernel, ssmem), name))) return r;
-  const int sblocks = (int)std::min<i64>(nrhs, (i64)nsm * 4);
+  const int sblocks = (int)std::min<i64>(nrhs, (i64)nsm);
   ds_b_to_r32_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, B, ldb, R32, W);
   if ((r = launch_status(name))) return r;
-  ds_solve_kernel<<<sblocks, 32, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
+  ds_solve_kernel<<<sblocks, 32 * kBsWarps, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
   if ((r = launch_status(name))) return r;
   ds_update_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, R32, X, ldx, 1, W);
   if ((r = launch_status(name))) return r;
@@ -307,7 +289,7 @@ static int dsgbsv_impl(i64 n, i64 kl, i64 ku, i64 nrhs, const double* AB, i64 ld
     ds_check_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, k, mx, tol, R, R32, W, iter, berr);
     if ((r = launch_status(name))) return r;
     if (k == mx) break;
-    ds_solve_kernel<<<sblocks, 32, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
+    ds_solve_kernel<<<sblocks, 32 * kBsWarps, ssmem, s>>>(n, (int)kl, (int)ku, nrhs, F, ldf, ipiv, R32, W, status_word());
     if ((r = launch_status(name))) return r;
     ds_update_kernel<<<eblocks, 256, 0, s>>>(n, nrhs, R32, X, ldx, 0, W);
     if ((r = launch_status(name))) return r;

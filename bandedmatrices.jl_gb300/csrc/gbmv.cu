@@ -177,6 +177,9 @@ __global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams
 
   // ------------------------------------------------------------------------ consumers
   const int ct = threadIdx.x - 32, bd = kGbmvThreads - 32;
+  // The tests of beta once, on the integer side: an FP64 comparison per output would
+  // occupy GB300's slow FP64 pipe, which the Float64 products already saturate.
+  const bool beta0 = p.beta == T(0);
   for (i64 k = 0; k < my_tiles; ++k) {
     const i64 t = (i64)blockIdx.x + k * (i64)gridDim.x;
     const int s = (int)(k % p.stages);
@@ -209,8 +212,8 @@ __global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams
         const bool two = t2 < nout;
         const bool full1 = (o0 + tt - kl >= 0) && (li + ku <= nmax);
         const bool full2 = two && (o0 + t2 - kl >= 0) && (li2 + ku <= nmax);
-        T acc1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + tt];
-        T acc2 = (two && p.beta != T(0)) ? p.beta * p.y[o0 + t2] : T(0);
+        T acc1 = beta0 ? T(0) : p.beta * p.y[o0 + tt];
+        T acc2 = (two && !beta0) ? p.beta * p.y[o0 + t2] : T(0);
         if (full1 && full2) {
           // two independent chains over all kb terms
           int ia = abase + (li - kl) * (lda - 1) + li, ix = xbase + li - kl;
@@ -279,10 +282,10 @@ __global__ void __launch_bounds__(kGbmvThreads) gbmv_tma_kernel(const GbmvParams
             }
           }
         }
-        const T y1 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + tt];
+        const T y1 = beta0 ? T(0) : p.beta * p.y[o0 + tt];
         p.y[o0 + tt] = fma(p.alpha, acc1, y1);
         if (two) {
-          const T y2 = (p.beta == T(0)) ? T(0) : p.beta * p.y[o0 + t2];
+          const T y2 = beta0 ? T(0) : p.beta * p.y[o0 + t2];
           p.y[o0 + t2] = fma(p.alpha, acc2, y2);
         }
       }

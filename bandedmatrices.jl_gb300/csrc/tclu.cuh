@@ -23,14 +23,16 @@
 //        columns j0+kvr .. j0+kvr+31 enter the free quarter, every window row (zero
 //        outside the band);
 //     3. partial-pivot LU of the R x 32 panel by the R/32 warps that hold a row each
-//        (a named barrier among them), while the other warps load the next panel's
-//        entering rows and columns into the staging buffer: the pivot is the
-//        largest |a| (exact to 2^-15 relative; the first row among near-equals), the
-//        interchange covers the step's columns onward, scaling by the rounded
-//        reciprocal, rank-1 update of the later panel columns;
-//     4. the panel's columns go to the FP32 factor storage as dgbtf2 leaves them
-//        (the layout gbtrs reads); then later interchanges are replayed on the L
-//        columns (dgetrf's order) for the update;
+//        (one named barrier among them per column): the pivot is the largest |a|
+//        (exact to 2^-15 relative; the first row among near-equals); rows do not
+//        move -- an interchange swaps the labels of the two window rows (it covers
+//        the step's columns onward), the pivot row is read in place; scaling by the
+//        rounded reciprocal, rank-1 update of the later panel columns; each column
+//        goes to the FP32 factor storage as soon as it is final, at the rows of its
+//        step (dgbtf2's layout, the one gbtrs reads); then every thread loads the
+//        next panel's entering rows and columns from the FP64 band;
+//     4. the panel's rows are put in their final order (every interchange applied,
+//        dgetrf's order) for the update;
 //     5. L21^T (R-32 rows x 32) is split into TF32 hi + lo (a = hi + lo, each rounded
 //        to nearest) as the B operand;
 //     6. each trailing quarter's warp applies the panel's interchanges to its TMEM
@@ -79,6 +81,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     sgbtrf_tc_kernel(i64 n, int kl, int ku, const double* __restrict__ A, i64 lda, float* __restrict__ F, i64 ldf,
                      i64* __restrict__ ipiv, i64* __restrict__ info, int* status) {
   extern __shared__ __align__(1024) unsigned char smem[];
+  if (!tc_lu_fits(kl, ku)) {  // the shared-memory layout and the TMEM ring assume these bounds
+    if (threadIdx.x == 0) *info = -2;
+    return;
+  }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int kv = kl + ku, klr = tc_klr(kl), kvr = tc_kvr(kl, ku), R = klr + kTcNB, RS = tc_rs(kl);
   const int nq = kvr / 32;  // trailing quarters per panel (1 .. 8)
@@ -88,8 +94,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 8);
   int* pivs = reinterpret_cast<int*>(smem + 64);              // [32] window-relative pivot rows
   uint32_t* wkey = reinterpret_cast<uint32_t*>(smem + 192);    // [2][8]
-  float* prow = reinterpret_cast<float*>(smem + 256);          // [2][32]
-  float* crow = reinterpret_cast<float*>(smem + 512);          // [2][32]
+  uint8_t* slot_of = smem + 256;                              // [2][256]: slot of window row r
   float* P = reinterpret_cast<float*>(smem + tc_off_P());      // [32][RS]: panel column c, window row r
   float* Aop = reinterpret_cast<float*>(smem + tc_off_A(kl));  // region g: hi at 8192 g floats, lo 4096 after
   float* Bhi = reinterpret_cast<float*>(smem + tc_off_B(kl));  // [klr x 32] operand layout
@@ -132,35 +137,41 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc::wait_st();
   }
   // The rows and columns panel (j1 / 32) brings in, from the FP64 band, rounded to FP32:
-  // rows j1+klr .. j1+klr+31 over its columns j1 .. j1+kvr-1, and the window's last 64
-  // rows over the 32 columns j1+kvr .. (the rows above are zero: outside the band).
-  // Threads lt = 0 .. nt-1 of the caller; eight loads in flight per thread.
-  auto stage = [&](i64 j1, int lt, int nt) {
-    const int tot_r = kvr * 32, tot = tot_r + 32 * 64;
-    for (int e0 = lt; e0 < tot; e0 += 8 * nt) {
-      float v[8];
+  // rows j1+klr .. j1+klr+31 over its columns j1 .. j1+kvr-1 into Srow (warp w, lane r:
+  // columns w, w+8, ..; 32 consecutive rows of a column per warp load), and the window's
+  // last 64 rows over the 32 columns j1+kvr .. into Scol (zero outside the band and the
+  // matrix).  Every thread issues its kStageRegs loads into registers, the panel
+  // factorization runs while they are in flight, then they are rounded and stored.
+  constexpr int kStageRegs = 40;
+  double sv[kStageRegs];
+  auto stage_issue = [&](i64 j1) {
+    const double* Ab = A + j1 * lda;                 // column j1
+    const int lim = (int)min(n - j1, (i64)1 << 30);  // rows / columns j1 + x exist for x < lim
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int e = e0 + q * nt;
-        v[q] = 0.0f;
-        if (e < tot_r) v[q] = aval(j1 + klr + (e & 31), j1 + (e >> 5));
-        else if (e < tot) {
-          const int f = e - tot_r;
-          v[q] = aval(j1 + klr - 32 + (f & 63), j1 + kvr + (f >> 6));
-        }
-      }
+    for (int q = 0; q < 32; ++q) {
+      const int cc = warp + 8 * q, ri = klr + lane, d = ri - cc;
+      sv[q] = (cc < kvr && ri < lim && cc < lim && d <= kl && d >= -ku) ? Ab[(ku + d) + (i64)cc * lda] : 0.0;
+    }
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int e = e0 + q * nt;
-        if (e < tot_r) Srow[(e >> 5) * 32 + ((e & 31) ^ ((e >> 5) & 31))] = v[q];
-        else if (e < tot) {
-          const int f = e - tot_r;
-          Scol[(f >> 6) * 64 + ((f & 63) ^ (f >> 6))] = v[q];
-        }
-      }
+    for (int q = 0; q < 8; ++q) {
+      const int f = tid + kTcThreads * q, ri = klr - 32 + (f & 63), ci = kvr + (f >> 6), d = ri - ci;
+      sv[32 + q] = (ri < lim && ci < lim && d <= kl && d >= -ku) ? Ab[(ku + d) + (i64)ci * lda] : 0.0;
     }
   };
-  stage(0, tid, kTcThreads);
+  auto stage_store = [&]() {
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int cc = warp + 8 * q;
+      if (cc < kvr) Srow[cc * 32 + (lane ^ (cc & 31))] = (float)sv[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int f = tid + kTcThreads * q;
+      Scol[(f >> 6) * 64 + ((f & 63) ^ (f >> 6))] = (float)sv[32 + q];
+    }
+  };
+  stage_issue(0);
+  stage_store();
   __syncthreads();
   long long inf = 0;  // thread 0
   i64 k = 0;
@@ -222,100 +233,78 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc::fence_after();
 
-    // ---- 3. panel LU, thread t = window row t, by the nw_lu warps (named barrier 1);
-    // meanwhile the other warps stage the next panel's rows and columns
-    if (warp >= nw_lu) {
-      stage(j0 + kTcNB, tid - 32 * nw_lu, kTcThreads - 32 * nw_lu);
-    } else {
-      float a[kTcNB];
-      const bool has_row = tid < R;
-#pragma unroll
-      for (int c = 0; c < kTcNB; ++c) a[c] = (has_row && c < jb) ? P[c * RS + tid] : 0.0f;
-#pragma unroll
-      for (int c = 0; c < kTcNB; ++c) {
-        if (c < jb) {
-          const int par = c & 1;
-          const bool cand = has_row && tid >= c && tid <= c + kl && j0 + tid < n;
-          uint32_t key = 0u;
-          if (cand) {
-            uint32_t m = __float_as_uint(a[c]) & 0x7fffffffu;
-            m = m > 0x7f800000u ? 0u : m;  // NaN never wins
-            key = (m & 0xffffff00u) | (uint32_t)(255 - tid);
-          }
-          key = __reduce_max_sync(0xffffffffu, key);
-          if (lane == 0) wkey[par * 8 + warp] = key;
-          lu_sync();
-          uint32_t best = wkey[par * 8];
-          for (int w2 = 1; w2 < nw_lu; ++w2) best = max(best, wkey[par * 8 + w2]);
-          const int p = 255 - (int)(best & 255u);
-          float* pr = prow + 32 * par;
-          float* cr = crow + 32 * par;
-          if (tid == p) {
-#pragma unroll
-            for (int c2 = c; c2 < kTcNB; ++c2) pr[c2] = a[c2];
-          }
-          if (tid == c && p != c) {
-#pragma unroll
-            for (int c2 = c; c2 < kTcNB; ++c2) cr[c2] = a[c2];
-          }
-          lu_sync();
-          const float pv = pr[c];
-          const bool nz = is_nonzero(pv);
-          if (tid == 0) {
-            ipiv[j0 + c] = j0 + p + 1;
-            pivs[c] = nz ? p : c;
-            if (!nz && inf == 0) inf = j0 + c + 1;
-          }
-          if (nz) {
-            if (p != c) {
-              if (tid == c) {
-#pragma unroll
-                for (int c2 = c; c2 < kTcNB; ++c2) a[c2] = pr[c2];
-              } else if (tid == p) {
-#pragma unroll
-                for (int c2 = c; c2 < kTcNB; ++c2) a[c2] = cr[c2];
-              }
-            }
-            if (has_row && tid > c && tid <= c + kl) {
-              const float l = a[c] * __frcp_rn(pv);
-              a[c] = l;
-#pragma unroll
-              for (int c2 = c + 1; c2 < kTcNB; ++c2) a[c2] = fmaf(-l, pr[c2], a[c2]);
-            }
-          }
-        } else if (tid == 0) {
-          pivs[c] = c;
+    // ---- 3. panel LU by the nw_lu warps, thread t holding slot t of the window (row t at
+    // the panel's start).  Rows never move: an interchange swaps the window rows' labels
+    // (lab: this slot's row; slot_of: the slot of a row, rewritten by every slot each
+    // column), the pivot row is read in place, and each column's values go to the factor
+    // storage as soon as they are final, at their row of that step -- dgbtf2's layout,
+    // where an interchange covers the step's columns onward.  One named barrier per
+    // column.  The pivot is the largest |a| (exact to 2^-15 relative), the first row
+    // among near-equals.
+    if (warp < nw_lu) {
+      int lab = tid;
+      bool moved = false;  // an interchange happened (warp-uniform)
+      slot_of[tid] = (uint8_t)tid;
+      lu_sync();
+      for (int c = 0; c < jb; ++c) {
+        const int par = c & 1;
+        const float* Pc = P + c * RS;
+        const bool cand = lab >= c && lab <= c + kl && j0 + lab < n;
+        uint32_t key = 0u;
+        if (cand) {
+          uint32_t m = __float_as_uint(Pc[tid]) & 0x7fffffffu;
+          m = m > 0x7f800000u ? 0u : m;  // NaN never wins
+          key = (m & 0xffffff00u) | (uint32_t)(255 - lab);
         }
-      }
-      if (has_row) {
-#pragma unroll
-        for (int c = 0; c < kTcNB; ++c) P[c * RS + tid] = a[c];
-      }
-    }
-    __syncthreads();
-    if (nw_lu == 8) {  // no spare warp: stage the next panel now
-      stage(j0 + kTcNB, tid, kTcThreads);
-      __syncthreads();
-    }
-    // ---- 4. panel columns to the factor storage (dgbtf2's layout), then the later
-    // interchanges on the L columns
-    for (int e = tid; e < kTcNB * R; e += kTcThreads) {
-      const int c = e / R, r = e - c * R;
-      const i64 col = j0 + c, i = j0 + r, d = i - col;
-      if (c < jb && i < n && d >= -kv && d <= kl) F[(kv + d) + col * ldf] = P[c * RS + r];
-    }
-    __syncthreads();
-    if (tid < jb) {
-      float* cl = P + tid * RS;
-      for (int c2 = tid + 1; c2 < jb; ++c2) {
-        const int p = pivs[c2];
-        if (p != c2) {
-          const float x = cl[c2];
-          cl[c2] = cl[p];
-          cl[p] = x;
+        key = __reduce_max_sync(0xffffffffu, key);
+        if (lane == 0) wkey[par * 8 + warp] = key;
+        lu_sync();
+        const uint32_t best = __reduce_max_sync(0xffffffffu, lane < nw_lu ? wkey[par * 8 + lane] : 0u);
+        const int p = 255 - (int)(best & 255u);  // the pivot row
+        const int ps = slot_of[par * 256 + p];   // and its slot
+        const float pv = Pc[ps];
+        const bool nz = is_nonzero(pv);
+        if (tid == 0) {
+          ipiv[j0 + c] = j0 + p + 1;
+          pivs[c] = nz ? p : c;
+          if (!nz && inf == 0) inf = j0 + c + 1;
         }
+        if (nz && p != c) {  // rows c and p trade places from this column on
+          if (lab == c) lab = p;
+          else if (lab == p) lab = c;
+          moved = true;
+        }
+        slot_of[(par ^ 1) * 256 + lab] = (uint8_t)tid;
+        float* Pt = P + tid;
+        if (nz && lab > c && lab <= c + kl && j0 + lab < n) {
+          // this row and the pivot row are different slots: declare it, so the loads of
+          // the loop need not wait for its stores
+          float* __restrict__ own = Pt;
+          const float* __restrict__ piv = P + ps;
+          const float l = own[c * RS] * __frcp_rn(pv);
+          own[c * RS] = l;
+#pragma unroll 4
+          for (int c2 = c + 1; c2 < kTcNB; ++c2) own[c2 * RS] = fmaf(-l, piv[c2 * RS], own[c2 * RS]);
+        }
+        // column c is final in this slot: to the factor storage at this step's row
+        const int d = lab - c;
+        if (d <= kl && j0 + lab < n) F[(kv + d) + (j0 + c) * ldf] = Pt[c * RS];
+      }
+      if (tid == 0)
+        for (int c = jb; c < kTcNB; ++c) pivs[c] = c;
+      if (moved) {  // the rows in their final order (every interchange applied), for the update
+        float row[kTcNB];
+#pragma unroll
+        for (int c2 = 0; c2 < kTcNB; ++c2) row[c2] = P[c2 * RS + tid];
+        lu_sync();
+#pragma unroll
+        for (int c2 = 0; c2 < kTcNB; ++c2) P[c2 * RS + lab] = row[c2];
       }
     }
+    // the next panel's entering rows and columns, loaded after the factorization: loads in
+    // flight during it saturated the SM's memory pipeline and slowed its shared-memory work
+    stage_issue(j0 + kTcNB);
+    stage_store();
     __syncthreads();
     // ---- 5. B operand: L21^T, rows r = 32 .. R-1 of the window (operand row r - 32)
     for (int e = tid; e < klr * kTcNB; e += kTcThreads) {

@@ -899,6 +899,13 @@ def main():
         stream = torch.cuda.current_stream(dev)
         bm = __import__("__graft_entry__").package()
         out["batched_solve"] = run_batched(bm, dev, stream)
+        bs = out["batched_solve"]
+        # the metric's other half: systems/s of the 4096-system batch, plain FP64 against
+        # the FP32-factor / FP64-refined solve at 1e-10 backward error
+        out["systems_per_s"] = {"plain_fp64": bs["plain_fp64"]["systems_per_s"],
+                                "refined_1e-10": bs["mixed_fp32_fp64_refined"]["systems_per_s"],
+                                "refined_vs_plain": bs["speedup_mixed_vs_plain"],
+                                "workload": bs["workload"]}
         torch.cuda.empty_cache()
         out["cpu_runnable"] = run_cpu_runnable(bm, dev, stream)
         out["qr_least_squares"] = run_qr(bm, dev, stream)

@@ -59,8 +59,8 @@ def test_sparse_bandwidths_and_back(bm, gpu):
         A = bm.from_sparse(S)
         assert A.bandwidths() == (l, u)
         assert torch.equal(A.to_dense().cpu(), torch.from_numpy(D))
-        with pytest.raises(ValueError):
-            bm.from_sparse(S, (max(l - 1, 0), u))
+        with pytest.raises(ValueError):  # one band narrower than S's: its nonzeros there are dropped
+            bm.from_sparse(S, (l - 1, u) if l > 0 else (l, u - 1))
     # explicit zeros do not count; an empty matrix has the bandwidths of Zeros
     Z = sp.csc_matrix((np.array([0.0, 0.0]), np.array([0, 5]), np.array([0, 1, 2] + [2] * 8)), shape=(10, 10))
     Sz = torch.sparse_csc_tensor(torch.from_numpy(Z.indptr.astype(np.int64)), torch.from_numpy(Z.indices.astype(np.int64)),
