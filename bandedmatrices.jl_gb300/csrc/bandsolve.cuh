@@ -196,6 +196,24 @@ __device__ bool bs_sweep(i64 n, int kl, int ku, const float* __restrict__ F, i64
             const int d = lane - t;
             if (d >= 1 && d <= KB) v = fmaf(-col0[t * cs + (FWD ? kv + d - seg0 : kv - d)], x, v);
           }
+        } else if (FWD && cols == 32 && remi >= KB + 31) {
+          // a full forward chunk with interchanges: by quarters of 8 steps, the quarters
+          // without one unrolled (most of them), the others through the general step
+          for (int q = 0; q < 4; ++q) {
+            const int t0 = 8 * q;
+            if (((swaps >> t0) & 0xffu) == 0u) {
+#pragma unroll
+              for (int k = 0; k < 8; ++k) {
+                const int t = t0 + k;
+                const float x = __shfl_sync(0xffffffffu, v, t);
+                const int d = lane - t;
+                if (d >= 1 && d <= KB) v = fmaf(-col0[t * cs + (kv + d - seg0)], x, v);
+              }
+            } else {
+#pragma unroll 1
+              for (int k = 0; k < 8; ++k) step(t0 + k, KB);
+            }
+          }
         } else {
 #pragma unroll 4
           for (int t = 0; t < cols; ++t) step(t, min(KB, remi - t));

@@ -26,12 +26,23 @@
 
 namespace bm {
 
+// Column stride of the QR window: >= l+1 and 4 (mod 32).  A warp's reflector
+// application reads eight columns with four threads each (rows r+sub, sub = 0..3), so
+// the column offsets 4c keep the 32 threads on distinct banks for 32-bit elements and
+// the 16 threads of each half-warp on distinct bank pairs for 64-bit ones.
+__host__ __device__ inline int qr_rs(int l) { return ((l + 1 + 27) & ~31) + 4; }
+template <int P>
+__host__ __device__ inline i64 gbqrf_smem_elems(int l, int u) {
+  const int K = u + 1;
+  return kHdr + (i64)qr_rs(l) * K + (i64)P * K + (l + 1);  // header + window + staging ring
+}
+
 template <typename T, int P, int G>
 __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 ldd, T* __restrict__ tau,
                             T* __restrict__ smem) {
   constexpr int NT = Grp<G>::NT;
   const int tid = Grp<G>::tid();
-  const int R = l + 1, K = u + 1, RS = lu_rs(l);
+  const int R = l + 1, K = u + 1, RS = qr_rs(l);
   T* hdr = smem;  // hdr[0] = tau_k, hdr[1] = xi1 (x1 + nu)
   T* W = smem + kHdr;
   T* S = W + (i64)RS * K;
@@ -93,8 +104,8 @@ __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 l
         }
       part += __shfl_xor_sync(0xffffffffu, part, 1);
       part += __shfl_xor_sync(0xffffffffu, part, 2);
+      T tk = T(0), xi1 = T(0);
       if (lane == 0) {
-        T tk = T(0), xi1 = T(0);
         if (scale != T(0)) {
           const T normu = !finite_nz ? scale : (direct ? sqrt(part) : scale * sqrt(part));
           const T x1 = x[pr0];
@@ -104,19 +115,22 @@ __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 l
           tk = xi1 / nu;
         }
         hdr[0] = tk;
-        hdr[1] = xi1;
         tau[k] = tk;
       }
+      tk = __shfl_sync(0xffffffffu, tk, 0);
+      xi1 = __shfl_sync(0xffffffffu, xi1, 0);
+      // the reflector x(2:len) / (x1 + nu), final: to the factor storage, with R(k,k)
+      if (xi1 != T(0) || tk != T(0))
+        for (int i = 1 + lane; i < len; i += 32) x[prow(i)] = x[prow(i)] / xi1;
+      __syncwarp();
+      for (int r = lane; r < len; r += 32) D[(u + r) + k * ldd] = x[prow(r)];
     }
     Grp<G>::sync();
-    const T tk = hdr[0], xi1 = hdr[1];
-    if (xi1 != T(0) || tk != T(0)) {
-      for (int i = 1 + tid; i < len; i += NT) x[prow(i)] = x[prow(i)] / xi1;
-    }
-    Grp<G>::sync();
+    const T tk = hdr[0];
     // ---- apply to columns k+1 .. k+min(u, n-1-k): four threads per column, the dot
     // product in four interleaved partial sums (rows 1+t, 5+t, ...) combined
-    // (s0+s1)+(s2+s3), then each thread updates its own rows
+    // (s0+s1)+(s2+s3), then each thread updates its own rows; row k of R is final and
+    // goes to the factor storage
     const int nc = (int)min((i64)u, n - 1 - k);
     const int sub = tid & 3;
     for (int base = 0; base < nc; base += NT / 4) {
@@ -133,25 +147,21 @@ __device__ void gbqrf_group(i64 m, i64 n, int l, int u, T* __restrict__ D, i64 l
       part += __shfl_xor_sync(0xffffffffu, part, 2);
       if (act) {
         const T v = tk * (a0 + part);
-        if (sub == 0) a[pr0] = a0 - v;
+        if (sub == 0) {
+          a[pr0] = a0 - v;
+          D[(u - c) + (k + c) * ldd] = a0 - v;
+        }
         for (int i = 1 + sub; i < len; i += 4) a[prow(i)] = fma(-v, x[prow(i)], a[prow(i)]);
       }
     }
-    Grp<G>::sync();
-    // ---- row k of R and the reflector of column k are final
-    const int ncw = (int)min((i64)u, n - 1 - k);
-    for (int c = tid; c <= ncw; c += NT) {
-      int pc = pc0 + c;
-      pc = pc >= K ? pc - K : pc;
-      D[(u - c) + (k + c) * ldd] = W[pr0 + pc * RS];
-    }
-    for (int r = 1 + tid; r < len; r += NT) D[(u + r) + k * ldd] = x[prow(r)];
-    Grp<G>::sync();
     if (k + 1 == ncols) break;
-    // ---- slide: row k+1+l enters physical row pr0, column k+1+u enters physical column pc0
-    for (int r = tid; r < R; r += NT) W[r + pc0 * RS] = T(0);
+    Grp<G>::sync();  // every read of column k and row k is done
+    // ---- slide: row k+1+l enters physical row pr0, column k+1+u enters physical column
+    // pc0 (zero above the entering row).  A thread stores the staged entries it copied
+    // itself, so its own wait is enough; the zeroing leaves row pr0 to the entering row.
+    for (int r = tid; r < R; r += NT)
+      if (r != pr0) W[r + pc0 * RS] = T(0);
     cp_async_wait<P - 1>();
-    Grp<G>::sync();
     const i64 inew = k + 1 + l;
     const T* st = S + (int)(inew & (P - 1)) * K;
     for (int c = tid; c < K; c += NT) {
@@ -246,7 +256,7 @@ static int gbqrf_impl(i64 m, i64 n, i64 l, i64 u, T* D, i64 ldd, T* tau, cudaStr
   if (ldd < l + u + 1) return -6;
   if (m == 0 || n == 0) return BM_OK;
   if (!tau) return -7;
-  const i64 bytes = gbtrf_smem_elems<4>((int)l, (int)u) * (i64)sizeof(T);
+  const i64 bytes = gbqrf_smem_elems<4>((int)l, (int)u) * (i64)sizeof(T);
   if (bytes > 227 * 1024) {
     set_error("%s: band (l=%lld, u=%lld) exceeds the window limit", name, (long long)l, (long long)u);
     return BM_ERR_UNSUPPORTED;

@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bool moved = false;  // an interchange happened (warp-uniform)
       slot_of[tid] = (uint8_t)tid;
       lu_sync();
+      float* Fcol = F + j0 * ldf + kv;  // row d of column j0 + c at Fcol[d] (advanced per column)
       for (int c = 0; c < jb; ++c) {
         const int par = c & 1;
         const float* Pc = P + c * RS;
@@ -288,7 +289,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         // column c is final in this slot: to the factor storage at this step's row
         const int d = lab - c;
-        if (d <= kl && j0 + lab < n) F[(kv + d) + (j0 + c) * ldf] = Pt[c * RS];
+        if (d <= kl && j0 + lab < n) Fcol[d] = Pt[c * RS];
+        Fcol += ldf;
       }
       if (tid == 0)
         for (int c = jb; c < kTcNB; ++c) pivs[c] = c;
