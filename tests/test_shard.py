@@ -1,8 +1,9 @@
 """The multi-GPU division of work, run as two gloo ranks on the CPU: gbmv row blocks
 with the x-halo exchange (each rank computes its rows from its band block with the
-oracle's gbmv; the gathered result equals the unsharded one bit for bit) and the
-batched solves' system assignment (a disjoint, balanced cover, identical on every
-rank)."""
+oracle's gbmv; the gathered result equals the unsharded one bit for bit), gbmm column
+blocks with the halo of A's storage columns (each rank's product of the blocks by the
+oracle's banded product equals the unsharded one bit for bit) and the batched solves'
+system assignment (a disjoint, balanced cover, identical on every rank)."""
 import os
 import socket
 import sys
@@ -53,6 +54,27 @@ def _rank_main(rank, port, outdir):
         dist.all_gather_object(parts, y)
         res[f"y{case}"] = np.concatenate(parts)
         res[f"yref{case}"] = oracle.gbmv("N", n, n, l, u, 1.0, data, x)
+    # gbmm by column blocks: the halo of A's storage columns, then the product of the blocks
+    for case, (n, Al, Au, Bl, Bu) in enumerate([(300, 3, 4, 2, 5), (37, 10, 2, 1, 12), (200, 0, 3, 4, 0)]):
+        rng = np.random.default_rng(400 + case)
+        Ad = np.asfortranarray(rng.standard_normal((Al + Au + 1, n)))
+        Bd = np.asfortranarray(rng.standard_normal((Bl + Bu + 1, n)))
+        Cl, Cu = Al + Bl, Au + Bu
+        j0, j1 = shard.row_ranges(n, WORLD)[rank]
+        blk = shard.col_block(n, Al, Au, Bl, Bu, j0, j1)
+        halo = shard.exchange_halo(torch.from_numpy(np.ascontiguousarray(Ad[:, j0:j1].T)), j0, j1, n, Bu, Bl, WORLD,
+                                   rank).numpy().T
+        assert np.array_equal(halo, Ad[:, blk["v0"]:blk["v1"]])
+        d, e = blk["d"], blk["e"]
+        mb = blk["i1"] - blk["i0"]
+        Cb = oracle.gbmm_generic(mb, blk["v1"] - blk["v0"], j1 - j0, Al + e, Au - e, Bl + d, Bu - d, Cl + d + e,
+                                 Cu - d - e, 1.0, np.asfortranarray(halo), np.asfortranarray(Bd[:, j0:j1]), 0.0,
+                                 np.zeros((Cl + Cu + 1, j1 - j0)))
+        parts = [None] * WORLD
+        dist.all_gather_object(parts, Cb)
+        res[f"C{case}"] = np.concatenate(parts, axis=1)
+        res[f"Cref{case}"] = oracle.gbmm_generic(n, n, n, Al, Au, Bl, Bu, Cl, Cu, 1.0, Ad, Bd, 0.0,
+                                                 np.zeros((Cl + Cu + 1, n)))
     rng = np.random.default_rng(5)
     cnt = 300
     n = np.exp(rng.uniform(np.log(64), np.log(4000), cnt)).astype(np.int64)
@@ -80,6 +102,8 @@ def test_two_rank_gbmv_halo_and_batched_shards(tmp_path):
         r = np.load(tmp_path / f"rank{rank}.npz", allow_pickle=True)
         for case in range(4):
             assert np.array_equal(r[f"y{case}"], r[f"yref{case}"]), (rank, case)
+        for case in range(3):
+            assert np.array_equal(r[f"C{case}"], r[f"Cref{case}"]), (rank, "gbmm", case)
         shards = [np.asarray(list(s), dtype=np.int64) for s in r["shards"]]
         allidx = np.sort(np.concatenate(shards))
         assert np.array_equal(allidx, np.arange(len(r["cost"])))  # disjoint cover
