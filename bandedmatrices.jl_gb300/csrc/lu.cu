@@ -40,21 +40,26 @@ __global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, in
 
 // ------------------------------------------------------------------ wide bands
 // Bands whose one-column window does not fit one CTA's shared memory (e.g. kl = ku =
-// 512 in Float64): the factorization runs panel by panel over the gbtrf storage in
-// global memory, as two launches per panel of kNB columns.
-//   * gbtrf_panel_kernel (one CTA): loads the panel -- rows j0 .. j0+kl+kNB-1 of its
-//     kNB columns -- into shared memory, takes dgbtf2's steps on it (pivot search,
-//     interchange within the panel's columns from the step's own column on, scaling,
-//     rank-1 update of the panel's later columns), stores it back (L in dgbtf2's
-//     format) with the pivots;
-//   * gbtrf_replay_kernel (one warp per column): every column the panel's steps can
-//     reach (up to kl+ku to its right) replays the steps in order -- interchange, then
-//     the update from the stored multipliers -- on its rows j0 .. j0+kl+kNB-1, kept in
-//     the warp's shared memory; the multipliers are staged once per CTA, and a step's
-//     interchange and zero-pivot flag come from ipiv and the stored U(j,j).
+// 128 or 512 in Float64): the factorization runs panel by panel over the gbtrf storage
+// in global memory, as two launches per panel of kNB columns.
+//   * gbtrf_panel_kernel (one CTA of 256 threads): loads the panel -- rows j0 ..
+//     j0+kl+kNB-1 of its kNB columns -- into shared memory and takes dgbtf2's steps on
+//     it: the pivot search (warp argmax, then across warps), the interchange within the
+//     panel's later columns, the reciprocal of the pivot (one thread), and the scaling
+//     and rank-1 update by one thread per row (rows beyond 256 wrap).  It stores the
+//     panel back (L in dgbtf2's format) with the pivots.
+//   * gbtrf_replay_kernel (one CTA of kReplayNT threads per column, one warp per
+//     sub-partition): every column the panel's steps can reach (up to kl+ku to its
+//     right) replays the steps in order on its rows j0 .. j0+kl+kNB-1, held in
+//     registers (row r by thread r mod kReplayNT).  At each step the threads holding the
+//     pivot row and row k publish both values through shared memory, one barrier, and
+//     every thread applies the interchange and its rows' fmas; the multipliers are
+//     staged once per CTA, and a step's interchange and zero-pivot flag come from ipiv
+//     and the stored U(j,j).
 // Each element therefore receives dgbtf2's sequence of operations: factors and pivots
 // equal the unblocked result bit for bit.
-constexpr int kWideWarps = 8;
+constexpr int kPanelNT = 256;
+constexpr int kReplayNT = 128;
 
 // the top kl rows of gbtrf storage (fill-in) start at zero, as dgbtrf sets them
 template <typename T>
@@ -66,36 +71,50 @@ __global__ void zero_fill_kernel(i64 n, int kl, T* ab, i64 ldab) {
   }
 }
 
+// Shared memory of the panel kernel: the panel (kNB columns of RS = (kl+kNB)|1
+// elements) and a header (per-warp keys and indices, the reciprocal of the pivot).
 template <typename T>
-__global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab, i64 ldab,
-                                                          i64* ipiv, i64* info) {
+__host__ __device__ constexpr i64 panel_smem_bytes(int kl) {
+  return (i64)((kl + kNB) | 1) * kNB * (i64)sizeof(T) + 256;
+}
+
+// Shared-memory panel, for bands whose panel rows exceed the register panels: the
+// panel in shared memory, one thread per row for the scaling and the update.
+template <typename T>
+__global__ void __launch_bounds__(kPanelNT) gbtrf_panel_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab,
+                                                                i64 ldab, i64* ipiv, i64* info) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NT = 256, NB = kNB;
+  constexpr int NT = kPanelNT, NB = kNB, NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, wig = tid >> 5;
   const int kv = kl + ku, R = kl + NB, RS = R | 1;
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
   T* P = reinterpret_cast<T*>(smem_raw);  // panel: column c (0..jb-1) x row r (matrix row j0 + r)
-  int* hdr = reinterpret_cast<int*>(P + (i64)RS * NB);  // [0] pivot, [4..] per-warp keys and indices
+  unsigned long long* wk = reinterpret_cast<unsigned long long*>(P + (i64)RS * NB);  // NW warp keys
+  int* wi = reinterpret_cast<int*>(wk + NW);                                          // NW warp indices
+  T* srcp = reinterpret_cast<T*>(wk + NW + NW / 2);                                   // 1 / pivot
   // entry (row j0+r, column j0+c) of the storage when it lies in it
   auto sidx = [&](int r, int c) -> i64 {
     const i64 i = j0 + r, col = j0 + c;
     const i64 d = i - col;
     return (i < m && d >= -kv && d <= kl) ? (kv + d) + col * ldab : (i64)-1;
   };
-  for (int e = tid; e < R * jb; e += NT) {
-    const int c = e / R, r = e - c * R;
-    const i64 g = sidx(r, c);
-    P[c * RS + r] = g >= 0 ? ab[g] : T(0);
-  }
-  __syncthreads();
+  for (int c = 0; c < jb; ++c)  // asynchronous element copies (zero outside the storage), one wait
+    for (int r = tid; r < R; r += NT) {
+      const i64 g = sidx(r, c);
+      cp_async_elem(P + c * RS + r, g >= 0 ? ab + g : ab, g >= 0);
+    }
+  cp_async_commit();
   i64 inf = *info;
+  cp_async_wait<0>();
+  __syncthreads();
   for (int c = 0; c < jb; ++c) {
     const i64 gj = j0 + c;
     const int km = (int)min((i64)kl, m - 1 - gj);
     T* colc = P + c * RS;
-    {  // idamax over rows c..c+km: every warp scans rows r = tid, tid+NT, ..., then the
-       // warps' (key, first index) pairs are combined (larger key, else smaller index)
+    // idamax over rows c..c+km: a warp argmax (first index on ties), then the warps'
+    // (key, index) pairs, combined the same way by every warp
+    {
       unsigned long long key = 0ull;
       int idx = 0x7fffffff;
       for (int r = tid; r <= km; r += NT) {
@@ -105,60 +124,49 @@ __global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, 
           idx = r;
         }
       }
-      const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
-      const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
-      const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
-      const int widx = (int)__reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? (unsigned)idx : 0x7fffffffu);
-      unsigned long long* wk = reinterpret_cast<unsigned long long*>(hdr + 4);  // 8 keys
-      int* wi = hdr + 4 + 2 * (NT / 32);                                         // 8 indices
+      const int widx = warp_argmax_first(key, idx);
       if (lane == 0) {
-        wk[wig] = ((unsigned long long)mhi << 32) | mlo;
+        wk[wig] = widx == 0x7fffffff ? 0ull : pivot_key(colc[c + widx], widx == 0);
         wi[wig] = widx;
       }
-      __syncthreads();
-      if (tid == 0) {
-        unsigned long long bk = wk[0];
-        int bi = wi[0];
-        for (int w = 1; w < NT / 32; ++w)
-          if (wi[w] != 0x7fffffff && (bi == 0x7fffffff || wk[w] > bk || (wk[w] == bk && wi[w] < bi))) {
-            bk = wk[w];
-            bi = wi[w];
-          }
-        hdr[0] = bi;
-        ipiv[gj] = gj + bi + 1;
-      }
     }
     __syncthreads();
-    const int jp = hdr[0];
+    const int jp = warp_argmax_first(lane < NW ? wk[lane] : 0ull, lane < NW ? wi[lane] : 0x7fffffff);
     const T piv = colc[c + jp];
-    const bool nonsingular = is_nonzero(piv);
-    if (nonsingular && jp != 0)
-      for (int t = c + tid; t < jb; t += NT) {
-        T* col = P + t * RS;
-        const T a = col[c];
-        col[c] = col[c + jp];
-        col[c + jp] = a;
-      }
-    __syncthreads();
-    if (nonsingular) {
-      const T rcp = T(1) / piv;
-      for (int r = 1 + tid; r <= km; r += NT) colc[c + r] = rcp * colc[c + r];
-    } else if (inf == 0) {
-      inf = gj + 1;
+    const bool ns = is_nonzero(piv);
+    if (tid == 0) {
+      ipiv[gj] = gj + jp + 1;
+      if (ns) *srcp = T(1) / piv;
+    }
+    if (!ns && inf == 0) inf = gj + 1;
+    // interchange of rows c and c+jp in the panel's later columns (warp 1); column c's
+    // own interchange is folded into the scaling below
+    if (ns && jp != 0 && tid >= 32 && tid - 32 < jb - 1 - c) {
+      T* col = P + (c + 1 + tid - 32) * RS;
+      const T a = col[c];
+      col[c] = col[c + jp];
+      col[c + jp] = a;
     }
     __syncthreads();
-    if (nonsingular) {  // rank-1 update of the panel's later columns: a thread per row
-      for (int r = c + 1 + tid; r <= c + km; r += NT) {
-        const T l = colc[r];
+    if (ns) {  // multipliers and the rank-1 update of the panel's later columns, by row
+      const T rcp = *srcp;
+      const T d0 = colc[c];  // row c's value before the interchange: it moves to row c+jp
+      for (int r = 1 + tid; r <= km; r += NT) {
+        const T l = rcp * (r == jp ? d0 : colc[c + r]);
+        colc[c + r] = l;
         for (int cc = c + 1; cc < jb; ++cc) {
           T* col = P + cc * RS;
           const T u = col[c];
-          if (is_nonzero(u)) col[r] = fma(l, -u, col[r]);
+          if (is_nonzero(u)) col[c + r] = fma(l, -u, col[c + r]);
         }
       }
     }
     __syncthreads();
+    // U(j, j): written after the barrier, as the scaling above still reads row c's
+    // old value; no thread reads column c again
+    if (tid == 0 && ns) colc[c] = piv;
   }
+  __syncthreads();
   for (int e = tid; e < R * jb; e += NT) {
     const int c = e / R, r = e - c * R;
     const i64 g = sidx(r, c);
@@ -167,94 +175,285 @@ __global__ void __launch_bounds__(256) gbtrf_panel_kernel(i64 m, i64 n, int kl, 
   if (tid == 0) *info = inf;
 }
 
-// One warp per column t = first + warp index: rows j0 .. j0+R-1 of the column replay
-// the panel's steps.  smem: the panel's multipliers (R x jb, staged per CTA) and one
-// R-row column buffer per warp.
+// Register panel: NT threads, thread t holds RPT rows of the panel's kNB columns in
+// registers, v[s][q] = (row ri[s], column c + q) at step c (the window rotates by one
+// column per step, and the finished column is stored).  Rows start as ri[s] = t + NT*s;
+// the row that becomes U's row at step c (row c, held by thread c in slot 0) then
+// rotates to the thread's last slot, so a thread's rows still in the active range
+// c+1 .. c+kl are always its slots 0 .. A-1, A = ceil(kl / NT): with kl <= NT every
+// thread updates one row per step, which spreads the FP64 work evenly over the warps.
+// A step: the rows' keys and a warp argmax, the warps' results through shared memory
+// (barrier 1); the threads holding the pivot row and row c publish both rows and the
+// reciprocal of the pivot (barrier 2); then row c takes the pivot row, the pivot row's
+// holder takes row c's values, and every thread scales and updates its active rows,
+// skipping columns whose U entry is zero (a mask the same for every thread).
+template <typename T, int NT, int RPT, int A>
+__global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab,
+                                                              i64 ldab, i64* ipiv, i64* info) {
+  constexpr int NB = kNB, NW = NT / 32;
+  static_assert(A <= RPT && NB <= NT, "panel layout");
+  __shared__ unsigned long long wk[2][NW];
+  __shared__ int wi[2][NW];
+  __shared__ T prow[2][NB], crow[2][NB], srcp[2];
+  const int tid = threadIdx.x, lane = tid & 31, wig = tid >> 5;
+  const int kv = kl + ku, R = kl + NB;
+  const i64 mn = min(m, n);
+  const int jb = (int)min((i64)NB, mn - j0);
+  T v[RPT][NB];
+  int ri[RPT];
+#pragma unroll
+  for (int s = 0; s < RPT; ++s) {
+    ri[s] = tid + NT * s;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const int r = ri[s], d = r - q;
+      const bool ok = q < jb && r < R && j0 + r < m && d >= -kv && d <= kl;
+      v[s][q] = ok ? ab[(kv + d) + (j0 + q) * ldab] : T(0);
+    }
+  }
+  i64 inf = *info;
+  for (int c = 0; c < jb; ++c) {
+    const i64 gj = j0 + c;
+    const int km = (int)min((i64)kl, m - 1 - gj);
+    const int par = c & 1;
+    // idamax over rows c..c+km (first index on ties)
+    unsigned long long key = 0ull;
+    int idx = 0x7fffffff;
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      const int r = ri[s];
+      if (r >= c && r <= c + km) {
+        const unsigned long long k = pivot_key(v[s][0], r == c);
+        if (idx == 0x7fffffff || k > key || (k == key && r - c < idx)) {
+          key = k;
+          idx = r - c;
+        }
+      }
+    }
+    const int widx = warp_argmax_first(key, idx);
+    const int src = widx == 0x7fffffff ? 0 : (c + widx) & 31;  // the lane holding the winner
+    const unsigned long long wkey = __shfl_sync(0xffffffffu, key, src);
+    if (lane == 0) {
+      wk[par][wig] = widx == 0x7fffffff ? 0ull : wkey;
+      wi[par][wig] = widx;
+    }
+    __syncthreads();
+    const int jp = warp_argmax_first(lane < NW ? wk[par][lane] : 0ull, lane < NW ? wi[par][lane] : 0x7fffffff);
+    const int rp = c + jp;
+    // the pivot row and row c (columns c .. c+NB-1 of the window), and 1/pivot
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      if (ri[s] == rp) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) prow[par][q] = v[s][q];
+        if (is_nonzero(v[s][0])) srcp[par] = T(1) / v[s][0];
+      }
+      if (ri[s] == c && jp != 0) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) crow[par][q] = v[s][q];
+      }
+    }
+    if (tid == 0) ipiv[gj] = gj + jp + 1;
+    __syncthreads();
+    const bool ns = is_nonzero(prow[par][0]);
+    if (!ns && inf == 0) inf = gj + 1;
+    if (ns) {
+      if (tid == c) {  // row c (slot 0) takes the pivot row and retires to the last slot
+#pragma unroll
+        for (int q = 0; q < NB; ++q) v[0][q] = prow[par][q];
+#pragma unroll
+        for (int s = 0; s + 1 < RPT; ++s) {
+          const int t = ri[s];
+          ri[s] = ri[s + 1];
+          ri[s + 1] = t;
+#pragma unroll
+          for (int q = 0; q < NB; ++q) {
+            const T x = v[s][q];
+            v[s][q] = v[s + 1][q];
+            v[s + 1][q] = x;
+          }
+        }
+      }
+      if (jp != 0) {  // the pivot row's holder takes row c's values
+#pragma unroll
+        for (int s = 0; s < A; ++s)
+          if (ri[s] == rp) {
+#pragma unroll
+            for (int q = 0; q < NB; ++q) v[s][q] = crow[par][q];
+          }
+      }
+      const T rcp = srcp[par];
+      const int nq = jb - c;  // columns of the panel from c on
+      T u[NB];
+      unsigned umask = 0u;  // columns q >= 1 of the panel with a nonzero U(c, c+q)
+#pragma unroll
+      for (int q = 1; q < NB; ++q) {
+        u[q] = prow[par][q];
+        umask |= (q < nq && is_nonzero(u[q])) ? (1u << q) : 0u;
+      }
+#pragma unroll
+      for (int s = 0; s < A; ++s) {
+        const int r = ri[s];
+        if (r > c && r <= c + km) {
+          const T l = rcp * v[s][0];
+          v[s][0] = l;
+#pragma unroll
+          for (int q = 1; q < NB; ++q)
+            if (umask & (1u << q)) v[s][q] = fma(l, -u[q], v[s][q]);
+        }
+      }
+    } else if (tid == c) {  // a zero pivot: row c retires unchanged
+#pragma unroll
+      for (int s = 0; s + 1 < RPT; ++s) {
+        const int t = ri[s];
+        ri[s] = ri[s + 1];
+        ri[s + 1] = t;
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+          const T x = v[s][q];
+          v[s][q] = v[s + 1][q];
+          v[s + 1][q] = x;
+        }
+      }
+    }
+    // column c is final: store it and rotate the window
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      const int r = ri[s], d = r - c;
+      if (r < R && j0 + r < m && d >= -kv && d <= kl) ab[(kv + d) + gj * ldab] = v[s][0];
+#pragma unroll
+      for (int q = 0; q < NB - 1; ++q) v[s][q] = v[s][q + 1];
+      v[s][NB - 1] = T(0);
+    }
+  }
+  if (tid == 0) *info = inf;
+}
+
+// Register panel shapes (threads, rows per thread, active rows per thread) by kl;
+// 0 where the shared-memory panel takes the band.
+struct PanelShape {
+  int nt, rpt, act;
+};
 template <typename T>
-__global__ void __launch_bounds__(32 * kWideWarps) gbtrf_replay_kernel(i64 m, i64 n, int kl, int ku, i64 j0,
-                                                                       i64 first, i64 last, T* ab, i64 ldab,
-                                                                       const i64* ipiv) {
+inline PanelShape panel_shape(i64 kl) {
+  const i64 R = kl + kNB;
+  if (R <= 128) return {128, 1, 1};
+  if (kl <= 128) return {128, 2, 1};
+  if (R <= 256) return {128, 2, 2};
+  if (R <= 384) return {128, 3, 3};
+  if (kl <= 512 && R <= 768) return {256, 3, 2};
+  if (R <= 768) return {256, 3, 3};
+  if (sizeof(T) == 4 && kl <= 768 && R <= 1024) return {256, 4, 3};
+  if (sizeof(T) == 4 && R <= 1024) return {256, 4, 4};
+  return {0, 0, 0};
+}
+
+// One CTA per column t = first + blockIdx.x; thread r mod kReplayNT holds rows j0 + r
+// (RPT of them) in registers.  smem: the panel's multipliers, L[k*RS + r] for the row
+// j0 + r at step k.
+template <typename T>
+__host__ __device__ constexpr i64 replay_smem_bytes(int kl) {
+  return (i64)((kl + kNB) | 1) * kNB * (i64)sizeof(T);
+}
+
+template <typename T, int RPT>
+__global__ void __launch_bounds__(kReplayNT) gbtrf_replay_kernel(i64 m, i64 n, int kl, int ku, i64 j0, i64 first,
+                                                                  T* ab, i64 ldab, const i64* ipiv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NB = kNB;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int NB = kNB, NT = kReplayNT;
+  __shared__ int st[NB];
+  __shared__ T xch[2][2];  // [step parity][0: the pivot row's value, 1: row k's value]
+  const int tid = threadIdx.x;
   const int kv = kl + ku, R = kl + NB, RS = R | 1;
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
-  T* L = reinterpret_cast<T*>(smem_raw);  // column k of the panel: L[k*RS + r], rows j0 + r
-  T* colbuf = L + (i64)RS * NB + (i64)w * RS;
-  __shared__ int st[kNB];
-  for (int e = threadIdx.x; e < R * jb; e += blockDim.x) {
-    const int k = e / R, r = e - k * R;
-    const i64 i = j0 + r, col = j0 + k, d = i - col;
-    L[k * RS + r] = (i < m && d >= -kv && d <= kl) ? ab[(kv + d) + col * ldab] : T(0);
+  const i64 t = first + blockIdx.x;
+  T* L = reinterpret_cast<T*>(smem_raw);
+  for (int k = 0; k < jb; ++k) {  // asynchronous element copies, one wait
+    const i64 gk = j0 + k;
+    const int km = (int)min((i64)kl, m - 1 - gk);
+    for (int i = tid; i < km; i += NT) cp_async_elem(L + k * RS + k + 1 + i, ab + (kv + 1 + i) + gk * ldab, true);
   }
-  if (threadIdx.x < jb) {  // -1: zero pivot (no interchange, no update)
-    const i64 gj = j0 + threadIdx.x;
-    st[threadIdx.x] = is_nonzero(ab[kv + gj * ldab]) ? (int)(ipiv[gj] - 1 - gj) : -1;
+  cp_async_commit();
+  if (tid < jb) {  // -1: zero pivot (no interchange, no update)
+    const i64 gj = j0 + tid;
+    st[tid] = is_nonzero(ab[kv + gj * ldab]) ? (int)(ipiv[gj] - 1 - gj) : -1;
   }
+  T v[RPT];
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + NT * i;
+    const i64 row = j0 + r, d = row - t;
+    v[i] = (r < R && row < m && d >= -kv && d <= kl) ? ab[(kv + d) + t * ldab] : T(0);
+  }
+  cp_async_wait<0>();
   __syncthreads();
-  for (i64 t = first + (i64)blockIdx.x * kWideWarps + w; t < last; t += (i64)gridDim.x * kWideWarps) {
-    // the column's rows j0 .. j0+R-1 (zero outside the storage)
-    for (int r = lane; r < R; r += 32) {
-      const i64 i = j0 + r, d = i - t;
-      colbuf[r] = (i < m && d >= -kv && d <= kl) ? ab[(kv + d) + t * ldab] : T(0);
-    }
-    __syncwarp();
-    for (int k = 0; k < jb; ++k) {
-      const int jp = st[k];
-      if (jp < 0) continue;  // zero pivot: no interchange, no update
-      T u = colbuf[k];
-      if (jp != 0) {
-        const T v = colbuf[k + jp];
-        __syncwarp();
-        if (lane == 0) {
-          colbuf[k + jp] = u;
-          colbuf[k] = v;
-        }
-        u = v;
-      }
-      __syncwarp();
-      if (is_nonzero(u)) {
-        const int km = (int)min((i64)kl, m - 1 - (j0 + k));
-        const T nu = -u;
-        const T* lk = L + k * RS;
-        // rows k+1+lane, +32, ...: eight loads issued before their fmas
-        int r = k + 1 + lane;
-        for (; r + 7 * 32 <= k + km; r += 8 * 32) {
-          T lv[8], av[8];
+  for (int k = 0; k < jb; ++k) {
+    const int jp = st[k];
+    if (jp < 0) continue;  // the same for every thread
+    const int par = k & 1;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            lv[q] = lk[r + 32 * q];
-            av[q] = colbuf[r + 32 * q];
-          }
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + NT * i;
+      if (r == k + jp) xch[par][0] = v[i];
+      if (r == k) xch[par][1] = v[i];
+    }
+    __syncthreads();
+    const T u = xch[par][0], a0 = xch[par][1];
+    const bool doit = is_nonzero(u);
+    const int km = (int)min((i64)kl, m - 1 - (j0 + k));
+    const T* lk = L + k * RS;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) colbuf[r + 32 * q] = fma(lv[q], nu, av[q]);
-        }
-        for (; r <= k + km; r += 32) colbuf[r] = fma(lk[r], nu, colbuf[r]);
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + NT * i;
+      if (r == k) {
+        v[i] = u;
+      } else if (r > k && r <= k + km) {
+        T a = r == k + jp ? a0 : v[i];
+        if (doit) a = fma(lk[r], -u, a);
+        v[i] = a;
       }
-      __syncwarp();
     }
-    for (int r = lane; r < R; r += 32) {
-      const i64 i = j0 + r, d = i - t;
-      if (i < m && d >= -kv && d <= kl) ab[(kv + d) + t * ldab] = colbuf[r];
-    }
-    __syncwarp();
   }
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + NT * i;
+    const i64 row = j0 + r, d = row - t;
+    if (r < R && row < m && d >= -kv && d <= kl) ab[(kv + d) + t * ldab] = v[i];
+  }
+}
+
+// rows held per replay thread: a class >= ceil((kl + kNB) / kReplayNT)
+inline int replay_rpt(i64 kl) {
+  const i64 r = ceil_div(kl + kNB, (i64)kReplayNT);
+  return r <= 1 ? 1 : r <= 2 ? 2 : r <= 3 ? 3 : r <= 4 ? 4 : r <= 5 ? 5 : r <= 6 ? 6 : r <= 8 ? 8 : r <= 12 ? 12 : 16;
 }
 
 template <typename T>
 static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
                            const char* name) {
-  const int R = (int)kl + kNB, RS = R | 1;
-  const i64 pbytes = (i64)RS * kNB * (i64)sizeof(T) + 256;  // panel + header (pivot, 8 warp keys/indices)
-  const i64 rbytes = ((i64)RS * kNB + (i64)RS * kWideWarps) * (i64)sizeof(T);
-  if (pbytes > 227 * 1024 || rbytes > 227 * 1024) {
+  const i64 pbytes = panel_smem_bytes<T>((int)kl), rbytes = replay_smem_bytes<T>((int)kl);
+  if (pbytes > 227 * 1024 || kl + kNB > 16 * kReplayNT) {
     set_error("%s: band (kl=%lld) exceeds the panel limit", name, (long long)kl);
     return BM_ERR_UNSUPPORTED;
   }
+  const int rpt = replay_rpt(kl);
+  // f(kernel) for the replay kernel of this band's row class
+  auto with_replay = [&](auto&& f) {
+    switch (rpt) {
+#define BM_RPT(v) \
+  case v:         \
+    return f(gbtrf_replay_kernel<T, v>);
+      BM_RPT(1) BM_RPT(2) BM_RPT(3) BM_RPT(4) BM_RPT(5) BM_RPT(6) BM_RPT(8) BM_RPT(12)
+#undef BM_RPT
+      default:
+        return f(gbtrf_replay_kernel<T, 16>);
+    }
+  };
+  const PanelShape ps = panel_shape<T>(kl);
   int r = cuda_status(ensure_smem((const void*)gbtrf_panel_kernel<T>, (int)pbytes), name);
   if (r) return r;
-  r = cuda_status(ensure_smem((const void*)gbtrf_replay_kernel<T>, (int)rbytes), name);
+  r = cuda_status(with_replay([&](auto kern) { return ensure_smem((const void*)kern, (int)rbytes); }), name);
   if (r) return r;
   r = cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
   if (r) return r;
@@ -266,13 +465,43 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
   const i64 mn = std::min(m, n);
   for (i64 j0 = 0; j0 < mn; j0 += kNB) {
     const i64 jb = std::min<i64>(kNB, mn - j0);
-    gbtrf_panel_kernel<T><<<1, 256, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+    {
+      const int code = ps.nt * 100 + ps.rpt * 10 + ps.act;
+      auto panel = [&](auto kern, int nt) {
+        kern<<<1, nt, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+      };
+      switch (code) {
+        case 12811: panel(gbtrf_panel_reg_kernel<T, 128, 1, 1>, 128); break;
+        case 12821: panel(gbtrf_panel_reg_kernel<T, 128, 2, 1>, 128); break;
+        case 12822: panel(gbtrf_panel_reg_kernel<T, 128, 2, 2>, 128); break;
+        case 12833: panel(gbtrf_panel_reg_kernel<T, 128, 3, 3>, 128); break;
+        case 25632: panel(gbtrf_panel_reg_kernel<T, 256, 3, 2>, 256); break;
+        case 25633: panel(gbtrf_panel_reg_kernel<T, 256, 3, 3>, 256); break;
+        case 25643:
+          if constexpr (sizeof(T) == 4) {
+            panel(gbtrf_panel_reg_kernel<T, 256, 4, 3>, 256);
+            break;
+          }
+          [[fallthrough]];
+        case 25644:
+          if constexpr (sizeof(T) == 4) {
+            panel(gbtrf_panel_reg_kernel<T, 256, 4, 4>, 256);
+            break;
+          }
+          [[fallthrough]];
+        default:
+          gbtrf_panel_kernel<T><<<1, kPanelNT, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv,
+                                                                      info);
+      }
+    }
     if ((r = launch_status(name))) return r;
     const i64 first = j0 + jb, last = std::min(n, j0 + jb + kl + ku);
     if (last > first) {
-      const i64 blocks = std::min<i64>(ceil_div(last - first, kWideWarps), (i64)num_sms() * 2);
-      gbtrf_replay_kernel<T><<<(unsigned)blocks, 32 * kWideWarps, (int)rbytes, stream>>>(
-          m, n, (int)kl, (int)ku, j0, first, last, ab, ldab, ipiv);
+      with_replay([&](auto kern) {
+        kern<<<(unsigned)(last - first), kReplayNT, (int)rbytes, stream>>>(m, n, (int)kl, (int)ku, j0, first, ab, ldab,
+                                                                          ipiv);
+        return 0;
+      });
       if ((r = launch_status(name))) return r;
     }
   }
@@ -313,8 +542,11 @@ __device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i
 // whose band exceeds the bounds its part's shared memory was sized for (wkl/wku,
 // nkl/nku), gets info[s] = -(field number) and is skipped; an order entry outside
 // [0, count) is skipped.
+// The 4-warp variant is held to three CTAs per SM (at most 170 registers a thread):
+// with more registers the CTAs per SM drop to two, which costs a quarter of the
+// batch's throughput.
 template <typename T, int W>
-__global__ void __launch_bounds__(32 * W) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
+__global__ void __launch_bounds__(32 * W, W == 4 ? 3 : 1) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
                                                              const int32_t* __restrict__ order, i64 n_wide, T* AB,
                                                              i64* ipiv, T* B, i64* info, int32_t* counter,
                                                              i64 narrow_elems, i64 wkl, i64 wku, i64 nkl, i64 nku) {

@@ -116,6 +116,45 @@ __device__ __forceinline__ unsigned long long pivot_key(float a, bool first) {
 __device__ __forceinline__ bool is_nonzero(double a) { return (abs_key(a)) != 0ull; }
 __device__ __forceinline__ bool is_nonzero(float a) { return (abs_key(a)) != 0ull; }
 
+// ---- division by a staged reciprocal (Float64)
+// On GB300's FP64 pipe a division costs about 570 cycles of latency and an fma 64.
+// Where the divisor d is known ahead of the step that divides by it (U(j,j) in a
+// solve), its reciprocal pair is staged off the critical path:
+//   yh = RN(1/d),  e = 1 - d*yh (exact, by fma),  yl = RN(e*yh),
+// and x/d, correctly rounded, then takes four dependent operations:
+//   t = RN(x*yl);  q0 = RN(x*yh + t);  r = x - d*q0 (exact);  q = RN(q0 + r*yh).
+// With Q = x/d in binade 2^eq and md the significand of d:
+//   * yh + yl is within 2^-105 |1/d| of 1/d, so q0 is within half an ulp of Q plus
+//     2^-50.4 of that, and r is exactly representable (a multiple of ulp(d) ulp(q0)
+//     below 2^53 of them);
+//   * q = RN(Q + r (yh - 1/d)), an error below md 2^(eq-107) (1 + 2^-50.4);
+//   * Q is at least 2^(eq-105)/md away from every midpoint between doubles (x - d*mid
+//     is a nonzero multiple of 2^(ed+eq-105), as mid has 54 significant bits);
+// so q = RN(Q) whenever md <= 2 - 2^-48 (Markstein's correction step; Muller et al.,
+// Handbook of Floating-Point Arithmetic, ch. 4).  That holds for every d but the 15
+// largest significands; those, subnormal or non-finite operands and exponents beyond
+// +-900 (where a step could underflow) take the plain x / d.
+__device__ __forceinline__ void div_rcp(double d, double& yh, double& yl) {
+  yh = 1.0 / d;
+  yl = fma(-d, yh, 1.0) * yh;
+}
+__device__ __forceinline__ double div_staged(double x, double d, double yh, double yl) {
+  const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long bd = (unsigned long long)__double_as_longlong(d);
+  const int ex = (int)((bx >> 52) & 0x7ff) - 1023, ed = (int)((bd >> 52) & 0x7ff) - 1023;
+  const bool ok = ex >= -900 && ex <= 900 && ed >= -900 && ed <= 900 && ex - ed >= -900 && ex - ed <= 900 &&
+                  (bd & 0xfffffffffffffull) <= 0xffffffffffff0ull;
+  if (!ok) return x / d;
+  const double q0 = fma(x, yh, x * yl);
+  const double r = fma(-d, q0, x);
+  return fma(r, yh, q0);
+}
+__device__ __forceinline__ void div_rcp(float d, float& yh, float& yl) {
+  yh = d;
+  yl = 0.0f;
+}
+__device__ __forceinline__ float div_staged(float x, float d, float, float) { return x / d; }
+
 // Warp argmax with the first index winning ties (idamax): every lane passes its best
 // (key, index); lanes with nothing to offer pass index 0x7fffffff.  Returns the winning
 // index to all lanes, using redux.sync on the integer pipe.
@@ -629,11 +668,12 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
       for (i64 j0 = 0; j0 < n - 1; j0 += kCh) {
         const int jn = (int)min((i64)kCh, n - 1 - j0);
         load_rows(kl, jn + kl, j0);
-        for (int e = tid; e < jn * kl; e += NT) {
-          const int sidx = e / kl, i = e - sidx * kl;
-          LC[sidx * kl + i] = (j0 + sidx + 1 + i < n) ? ab[(kv + 1 + i) + (j0 + sidx) * ldab] : T(0);
-        }
+        for (int sidx = 0; sidx < jn; ++sidx)
+          for (int i = tid; i < kl; i += NT)
+            cp_async_elem(LC + sidx * kl + i, ab + (kv + 1 + i) + (j0 + sidx) * ldab, j0 + sidx + 1 + i < n);
+        cp_async_commit();
         for (int sidx = tid; sidx < jn; sidx += NT) IP[sidx] = ipiv[j0 + sidx] - 1 - j0;
+        cp_async_wait<0>();
         gsync();
         if (nw > 0) {
           for (int st = 0; st < jn; ++st) {
@@ -649,7 +689,7 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
             }
             if (cok) {
               const T bj = X[st * nr + cl];
-              if (bj != T(0)) {
+              if (is_nonzero(bj)) {
                 const T t = -bj;
                 for (int i = r0; i < lm; i += rstep)
                   X[(st + 1 + i) * nr + cl] = fma(LC[st * kl + i], t, X[(st + 1 + i) * nr + cl]);
@@ -675,11 +715,15 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     while (true) {
       const int jn = (int)min((i64)kCh, j1 + 1);
       // U(j-i, j) = ab[(kv-i) + j*ldab], i = 0..kv, for j = j1, j1-1, ...
-      for (int e = tid; e < jn * (kv + 1); e += NT) {
-        const int t = e / (kv + 1), i = e - t * (kv + 1);
+      for (int t = 0; t < jn; ++t) {
         const i64 j = j1 - t;
-        LC[e] = (j - i >= 0) ? ab[(kv - i) + j * ldab] : T(0);
+        for (int i = tid; i <= kv; i += NT) cp_async_elem(LC + t * (kv + 1) + i, ab + (kv - i) + j * ldab, j - i >= 0);
       }
+      cp_async_commit();
+      // the reciprocal pairs of the chunk's U(j, j), in the pivot slots (unused here)
+      T* RH = reinterpret_cast<T*>(IP);
+      for (int t = tid; t < jn; t += NT) div_rcp(ab[kv + (j1 - t) * ldab], RH[t], RH[kChunk + t]);
+      cp_async_wait<0>();
       gsync();
       if (nw > 0) {
         for (int t = 0; t < jn; ++t) {
@@ -687,12 +731,12 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
           const int xs = (int)(j - base);
           if (own) {
             const T xv = X[xs * nr + oc];
-            if (xv != T(0)) X[xs * nr + oc] = xv / LC[t * (kv + 1)];
+            if (is_nonzero(xv)) X[xs * nr + oc] = div_staged(xv, LC[t * (kv + 1)], RH[t], RH[kChunk + t]);
           }
           wsync();
           if (cok) {
             const T xj = X[xs * nr + cl];
-            if (xj != T(0)) {
+            if (is_nonzero(xj)) {
               const T tt = -xj;
               const int lim = (int)min((i64)kv, j);
               for (int i = 1 + r0; i <= lim; i += rstep)
@@ -719,16 +763,20 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
     for (i64 j0 = 0; j0 < n; j0 += kCh) {
       const int jn = (int)min((i64)kCh, n - j0);
       // row i of U: U(i, i+c) = ab[(kv-c) + (i+c)*ldab], c = 0..kv
-      for (int e = tid; e < jn * (kv + 1); e += NT) {
-        const int t = e / (kv + 1), c = e - t * (kv + 1);
+      for (int t = 0; t < jn; ++t) {
         const i64 i = j0 + t;
-        LC[e] = (i + c < n) ? ab[(kv - c) + (i + c) * ldab] : T(0);
+        for (int c = tid; c <= kv; c += NT)
+          cp_async_elem(LC + t * (kv + 1) + c, i + c < n ? ab + (kv - c) + (i + c) * ldab : ab, i + c < n);
       }
+      cp_async_commit();
+      T* RH = reinterpret_cast<T*>(IP);
+      for (int t = tid; t < jn; t += NT) div_rcp(ab[kv + (j0 + t) * ldab], RH[t], RH[kChunk + t]);
+      cp_async_wait<0>();
       gsync();
       if (nw > 0) {
         for (int t = 0; t < jn; ++t) {
           const i64 i = j0 + t;
-          if (own) X[t * nr + oc] = X[t * nr + oc] / LC[t * (kv + 1)];
+          if (own) X[t * nr + oc] = div_staged(X[t * nr + oc], LC[t * (kv + 1)], RH[t], RH[kChunk + t]);
           wsync();
           if (cok) {
             const T xi = X[t * nr + cl];
@@ -756,12 +804,13 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
       load_rows(0, jn + kl, base);
       while (true) {
         // LC[t][i] = L(j+1+i, j), j = j1 - t; IP[t] = pivot row of j, in the window
-        for (int e = tid; e < jn * kl; e += NT) {
-          const int t = e / kl, i = e - t * kl;
+        for (int t = 0; t < jn; ++t) {
           const i64 j = j1 - t;
-          LC[e] = (j + 1 + i < n) ? ab[(kv + 1 + i) + j * ldab] : T(0);
+          for (int i = tid; i < kl; i += NT) cp_async_elem(LC + t * kl + i, ab + (kv + 1 + i) + j * ldab, j + 1 + i < n);
         }
+        cp_async_commit();
         for (int t = tid; t < jn; t += NT) IP[t] = ipiv[j1 - t] - 1 - base;
+        cp_async_wait<0>();
         gsync();
         if (nw > 0) {
           for (int t = 0; t < jn; ++t) {

@@ -349,10 +349,19 @@ def test_cta_lu_panels_singular_and_rectangular(bm, gpu, orc, dt, m, n, l, u, ze
 @pytest.mark.parametrize("dt,m,n,l,u,zero_cols", [(np.float64, 1500, 1500, 150, 150, ()),
                                                   (np.float64, 700, 600, 140, 160, (33, 300)),
                                                   (np.float32, 900, 900, 250, 240, (17,)),
-                                                  (np.float64, 600, 700, 200, 100, ())])
+                                                  (np.float64, 600, 700, 200, 100, ()),
+                                                  (np.float64, 700, 700, 300, 60, (45,)),
+                                                  (np.float64, 900, 900, 520, 30, (5, 600)),
+                                                  (np.float32, 800, 800, 700, 20, ()),
+                                                  (np.float32, 1000, 1000, 900, 10, ()),
+                                                  (np.float64, 900, 900, 800, 10, (3,)),
+                                                  (np.float64, 800, 800, 100, 300, ()),
+                                                  (np.float64, 1000, 1000, 128, 128, (77,)),
+                                                  (np.float64, 1200, 1100, 512, 40, ())])
 def test_wide_band_panels_bitexact(bm, gpu, orc, dt, m, n, l, u, zero_cols):
     """Bands whose one-column window exceeds shared memory go through the panel +
-    per-column replay launches: factors, pivots and info equal dgbtf2's bit for bit,
+    per-column replay launches (register panels of 1-4 rows per thread, and the
+    shared-memory panel beyond): factors, pivots and info equal dgbtf2's bit for bit,
     and square systems solve ('N' bit-exact, 'T' to 1e-12 / 1e-5)."""
     rng = np.random.default_rng(m + n + l + u)
     data = rng.standard_normal((l + u + 1, n)).astype(dt)
