@@ -175,23 +175,20 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_kernel(i64 m, i64 n, int
   if (tid == 0) *info = inf;
 }
 
-// Register panel: NT threads, thread t holds RPT rows of the panel's kNB columns in
-// registers, v[s][q] = (row ri[s], column c + q) at step c (the window rotates by one
-// column per step, and the finished column is stored).  Rows start as ri[s] = t + NT*s;
-// the row that becomes U's row at step c (row c, held by thread c in slot 0) then
-// rotates to the thread's last slot, so a thread's rows still in the active range
-// c+1 .. c+kl are always its slots 0 .. A-1, A = ceil(kl / NT): with kl <= NT every
-// thread updates one row per step, which spreads the FP64 work evenly over the warps.
-// A step: the rows' keys and a warp argmax, the warps' results through shared memory
-// (barrier 1); the threads holding the pivot row and row c publish both rows and the
-// reciprocal of the pivot (barrier 2); then row c takes the pivot row, the pivot row's
-// holder takes row c's values, and every thread scales and updates its active rows,
-// skipping columns whose U entry is zero (a mask the same for every thread).
-template <typename T, int NT, int RPT, int A>
-__global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab,
-                                                              i64 ldab, i64* ipiv, i64* info) {
-  constexpr int NB = kNB, NW = NT / 32;
-  static_assert(A <= RPT && NB <= NT, "panel layout");
+// Register panel (R = kl + kNB <= RPT * kPanelNT rows): thread t holds rows t + kPanelNT*i
+// of the panel's columns in registers, the column of the current step at index 0 (the
+// window rotates by one column per step, and the finished column is stored).  A step:
+// the key of each row, a warp argmax, the warps' results through shared memory (one
+// barrier); the threads holding the pivot row and row c publish both rows and the
+// reciprocal of the pivot (a second barrier); then every thread scales and updates its
+// own rows.  One CTA, so the panel's steps cost two barriers each and no shared-memory
+// traffic for the elements themselves.  (Measured against two alternatives at
+// kl = 128: four warps with two rows per thread, 41 us per panel, and rows rotating
+// out of the active slots with a uniform zero mask, 45 us, against 33 us for this one.)
+template <typename T, int RPT>
+__global__ void __launch_bounds__(kPanelNT) gbtrf_panel_reg_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab,
+                                                                    i64 ldab, i64* ipiv, i64* info) {
+  constexpr int NT = kPanelNT, NB = kNB, NW = NT / 32;
   __shared__ unsigned long long wk[2][NW];
   __shared__ int wi[2][NW];
   __shared__ T prow[2][NB], crow[2][NB], srcp[2];
@@ -199,18 +196,15 @@ __global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int k
   const int kv = kl + ku, R = kl + NB;
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
-  T v[RPT][NB];
-  int ri[RPT];
+  T v[RPT][NB];  // v[i][q]: row tid + NT*i of column c + q at step c
 #pragma unroll
-  for (int s = 0; s < RPT; ++s) {
-    ri[s] = tid + NT * s;
+  for (int i = 0; i < RPT; ++i)
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
-      const int r = ri[s], d = r - q;
+      const int r = tid + NT * i, d = r - q;
       const bool ok = q < jb && r < R && j0 + r < m && d >= -kv && d <= kl;
-      v[s][q] = ok ? ab[(kv + d) + (j0 + q) * ldab] : T(0);
+      v[i][q] = ok ? ab[(kv + d) + (j0 + q) * ldab] : T(0);
     }
-  }
   i64 inf = *info;
   for (int c = 0; c < jb; ++c) {
     const i64 gj = j0 + c;
@@ -220,11 +214,11 @@ __global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int k
     unsigned long long key = 0ull;
     int idx = 0x7fffffff;
 #pragma unroll
-    for (int s = 0; s < RPT; ++s) {
-      const int r = ri[s];
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + NT * i;
       if (r >= c && r <= c + km) {
-        const unsigned long long k = pivot_key(v[s][0], r == c);
-        if (idx == 0x7fffffff || k > key || (k == key && r - c < idx)) {
+        const unsigned long long k = pivot_key(v[i][0], r == c);
+        if (idx == 0x7fffffff || k > key) {
           key = k;
           idx = r - c;
         }
@@ -242,15 +236,16 @@ __global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int k
     const int rp = c + jp;
     // the pivot row and row c (columns c .. c+NB-1 of the window), and 1/pivot
 #pragma unroll
-    for (int s = 0; s < RPT; ++s) {
-      if (ri[s] == rp) {
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + NT * i;
+      if (r == rp) {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) prow[par][q] = v[s][q];
-        if (is_nonzero(v[s][0])) srcp[par] = T(1) / v[s][0];
+        for (int q = 0; q < NB; ++q) prow[par][q] = v[i][q];
+        if (is_nonzero(v[i][0])) srcp[par] = T(1) / v[i][0];
       }
-      if (ri[s] == c && jp != 0) {
+      if (r == c && jp != 0) {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) crow[par][q] = v[s][q];
+        for (int q = 0; q < NB; ++q) crow[par][q] = v[i][q];
       }
     }
     if (tid == 0) ipiv[gj] = gj + jp + 1;
@@ -258,94 +253,41 @@ __global__ void __launch_bounds__(NT) gbtrf_panel_reg_kernel(i64 m, i64 n, int k
     const bool ns = is_nonzero(prow[par][0]);
     if (!ns && inf == 0) inf = gj + 1;
     if (ns) {
-      if (tid == c) {  // row c (slot 0) takes the pivot row and retires to the last slot
-#pragma unroll
-        for (int q = 0; q < NB; ++q) v[0][q] = prow[par][q];
-#pragma unroll
-        for (int s = 0; s + 1 < RPT; ++s) {
-          const int t = ri[s];
-          ri[s] = ri[s + 1];
-          ri[s + 1] = t;
-#pragma unroll
-          for (int q = 0; q < NB; ++q) {
-            const T x = v[s][q];
-            v[s][q] = v[s + 1][q];
-            v[s + 1][q] = x;
-          }
-        }
-      }
-      if (jp != 0) {  // the pivot row's holder takes row c's values
-#pragma unroll
-        for (int s = 0; s < A; ++s)
-          if (ri[s] == rp) {
-#pragma unroll
-            for (int q = 0; q < NB; ++q) v[s][q] = crow[par][q];
-          }
-      }
       const T rcp = srcp[par];
       const int nq = jb - c;  // columns of the panel from c on
       T u[NB];
-      unsigned umask = 0u;  // columns q >= 1 of the panel with a nonzero U(c, c+q)
 #pragma unroll
-      for (int q = 1; q < NB; ++q) {
-        u[q] = prow[par][q];
-        umask |= (q < nq && is_nonzero(u[q])) ? (1u << q) : 0u;
-      }
+      for (int q = 1; q < NB; ++q) u[q] = prow[par][q];
 #pragma unroll
-      for (int s = 0; s < A; ++s) {
-        const int r = ri[s];
-        if (r > c && r <= c + km) {
-          const T l = rcp * v[s][0];
-          v[s][0] = l;
+      for (int i = 0; i < RPT; ++i) {
+        const int r = tid + NT * i;
+        if (r == c) {  // row c takes the pivot row
+#pragma unroll
+          for (int q = 0; q < NB; ++q) v[i][q] = prow[par][q];
+        } else if (r > c && r <= c + km) {
+          const bool sw = r == rp;  // this row takes row c's values
+          const T l = rcp * (sw ? crow[par][0] : v[i][0]);
+          v[i][0] = l;
 #pragma unroll
           for (int q = 1; q < NB; ++q)
-            if (umask & (1u << q)) v[s][q] = fma(l, -u[q], v[s][q]);
-        }
-      }
-    } else if (tid == c) {  // a zero pivot: row c retires unchanged
-#pragma unroll
-      for (int s = 0; s + 1 < RPT; ++s) {
-        const int t = ri[s];
-        ri[s] = ri[s + 1];
-        ri[s + 1] = t;
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-          const T x = v[s][q];
-          v[s][q] = v[s + 1][q];
-          v[s + 1][q] = x;
+            if (q < nq) {
+              const T a = sw ? crow[par][q] : v[i][q];
+              v[i][q] = is_nonzero(u[q]) ? fma(l, -u[q], a) : a;
+            }
         }
       }
     }
     // column c is final: store it and rotate the window
 #pragma unroll
-    for (int s = 0; s < RPT; ++s) {
-      const int r = ri[s], d = r - c;
-      if (r < R && j0 + r < m && d >= -kv && d <= kl) ab[(kv + d) + gj * ldab] = v[s][0];
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + NT * i, d = r - c;
+      if (r < R && j0 + r < m && d >= -kv && d <= kl) ab[(kv + d) + gj * ldab] = v[i][0];
 #pragma unroll
-      for (int q = 0; q < NB - 1; ++q) v[s][q] = v[s][q + 1];
-      v[s][NB - 1] = T(0);
+      for (int q = 0; q < NB - 1; ++q) v[i][q] = v[i][q + 1];
+      v[i][NB - 1] = T(0);
     }
   }
   if (tid == 0) *info = inf;
-}
-
-// Register panel shapes (threads, rows per thread, active rows per thread) by kl;
-// 0 where the shared-memory panel takes the band.
-struct PanelShape {
-  int nt, rpt, act;
-};
-template <typename T>
-inline PanelShape panel_shape(i64 kl) {
-  const i64 R = kl + kNB;
-  if (R <= 128) return {128, 1, 1};
-  if (kl <= 128) return {128, 2, 1};
-  if (R <= 256) return {128, 2, 2};
-  if (R <= 384) return {128, 3, 3};
-  if (kl <= 512 && R <= 768) return {256, 3, 2};
-  if (R <= 768) return {256, 3, 3};
-  if (sizeof(T) == 4 && kl <= 768 && R <= 1024) return {256, 4, 3};
-  if (sizeof(T) == 4 && R <= 1024) return {256, 4, 4};
-  return {0, 0, 0};
 }
 
 // One CTA per column t = first + blockIdx.x; thread r mod kReplayNT holds rows j0 + r
@@ -450,7 +392,10 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
         return f(gbtrf_replay_kernel<T, 16>);
     }
   };
-  const PanelShape ps = panel_shape<T>(kl);
+  // the register panel where the panel's rows fit RPT rows per thread (at most 3 in
+  // Float64, 4 in Float32, within the register file); else the shared-memory panel
+  const int prpt_need = (int)ceil_div(kl + kNB, (i64)kPanelNT);
+  const int prpt = prpt_need <= (sizeof(T) == 8 ? 3 : 4) ? prpt_need : 0;
   int r = cuda_status(ensure_smem((const void*)gbtrf_panel_kernel<T>, (int)pbytes), name);
   if (r) return r;
   r = cuda_status(with_replay([&](auto kern) { return ensure_smem((const void*)kern, (int)rbytes); }), name);
@@ -465,34 +410,24 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
   const i64 mn = std::min(m, n);
   for (i64 j0 = 0; j0 < mn; j0 += kNB) {
     const i64 jb = std::min<i64>(kNB, mn - j0);
-    {
-      const int code = ps.nt * 100 + ps.rpt * 10 + ps.act;
-      auto panel = [&](auto kern, int nt) {
-        kern<<<1, nt, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
-      };
-      switch (code) {
-        case 12811: panel(gbtrf_panel_reg_kernel<T, 128, 1, 1>, 128); break;
-        case 12821: panel(gbtrf_panel_reg_kernel<T, 128, 2, 1>, 128); break;
-        case 12822: panel(gbtrf_panel_reg_kernel<T, 128, 2, 2>, 128); break;
-        case 12833: panel(gbtrf_panel_reg_kernel<T, 128, 3, 3>, 128); break;
-        case 25632: panel(gbtrf_panel_reg_kernel<T, 256, 3, 2>, 256); break;
-        case 25633: panel(gbtrf_panel_reg_kernel<T, 256, 3, 3>, 256); break;
-        case 25643:
-          if constexpr (sizeof(T) == 4) {
-            panel(gbtrf_panel_reg_kernel<T, 256, 4, 3>, 256);
-            break;
-          }
-          [[fallthrough]];
-        case 25644:
-          if constexpr (sizeof(T) == 4) {
-            panel(gbtrf_panel_reg_kernel<T, 256, 4, 4>, 256);
-            break;
-          }
-          [[fallthrough]];
-        default:
-          gbtrf_panel_kernel<T><<<1, kPanelNT, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv,
-                                                                      info);
-      }
+    switch (prpt) {
+      case 1:
+        gbtrf_panel_reg_kernel<T, 1><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        break;
+      case 2:
+        gbtrf_panel_reg_kernel<T, 2><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        break;
+      case 3:
+        gbtrf_panel_reg_kernel<T, 3><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        break;
+      case 4:
+        if constexpr (sizeof(T) == 4) {
+          gbtrf_panel_reg_kernel<T, 4><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+          break;
+        }
+        [[fallthrough]];
+      default:
+        gbtrf_panel_kernel<T><<<1, kPanelNT, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
     }
     if ((r = launch_status(name))) return r;
     const i64 first = j0 + jb, last = std::min(n, j0 + jb + kl + ku);

@@ -428,3 +428,53 @@ def test_plan_matches_the_regular_batched_solve(bm, gpu):
     torch.cuda.synchronize()
     assert torch.equal(batch.X, X_ref)
     mp.close()
+
+
+def _hard_quotients(rng, count):
+    """(b, d) pairs whose quotient b/d lies within about eps * 2^-54 of an ulp from a
+    rounding midpoint: for an odd 53-bit D and a small odd eps, M = eps / D mod 2^54 is
+    odd and M*D = eps + B*2^54, so B/D = M/2^54 - eps/(D*2^54) with M/2^54 halfway
+    between two doubles.  A quarter of the pairs instead has divisors with the largest
+    significands, exponents beyond +-900 or subnormal numerators, where the solves take
+    the plain division."""
+    b = np.empty(count)
+    d = np.empty(count)
+    i = 0
+    while i < count:
+        D = int(rng.integers(2 ** 52, 2 ** 53)) | 1
+        eps = int(rng.choice([-7, -5, -3, -1, 1, 3, 5, 7]))
+        M = (eps * pow(D, -1, 2 ** 54)) % 2 ** 54
+        B, rem = divmod(M * D - eps, 2 ** 54)
+        if rem or not (2 ** 53 <= M < 2 ** 54 and 2 ** 52 <= B < 2 ** 53):
+            continue
+        e1, e2 = (int(x) for x in rng.integers(-200, 200, 2))
+        b[i] = np.ldexp(float(B), e1) * (1 if rng.random() < 0.5 else -1)
+        d[i] = np.ldexp(float(D), e2)
+        i += 1
+    k = count // 16
+    d[:k] = np.ldexp(2.0 - np.arange(k) % 20 * 2.0 ** -52, rng.integers(-30, 30, k))  # top significands
+    d[k:2 * k] *= 2.0 ** 700  # exponents beyond +-900
+    b[2 * k:3 * k] = rng.standard_normal(k) * 2.0 ** -1030  # subnormal numerators
+    b[3 * k:4 * k] = rng.standard_normal(k)
+    d[3 * k:4 * k] = rng.standard_normal(k)
+    return b, d
+
+
+@pytest.mark.parametrize("ku", [0, 3, 200])
+def test_solve_division_is_correctly_rounded(bm, gpu, orc, ku):
+    """The back substitution divides by U(j, j) through a staged reciprocal pair
+    (Markstein's correction step) outside the ranges where it takes the plain division;
+    on diagonal systems whose quotients sit next to rounding midpoints, 'N' and 'T'
+    solves equal IEEE division bit for bit."""
+    rng = np.random.default_rng(17 + ku)
+    n = 4096
+    b, d = _hard_quotients(rng, n)
+    data = np.zeros((ku + 1, n))
+    data[ku] = d
+    A = dev_band(bm, data, n, 0, ku, gpu)
+    F = bm.lu(A)
+    assert F.info == 0
+    want = b / d
+    bd = torch.from_numpy(b.copy()).to(gpu)
+    assert np.array_equal(F.solve(bd).cpu().numpy().view(np.int64), want.view(np.int64))
+    assert np.array_equal(F.T.solve(bd).cpu().numpy().view(np.int64), want.view(np.int64))
