@@ -537,6 +537,8 @@ static int gbtrf_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, 
   if (!info) return -8;
   if (m == 0 || n == 0) return cuda_status(cudaMemsetAsync(info, 0, sizeof(i64), stream), name);
   if (!ipiv) return -7;
+  // tiny bands: one warp, a lane per window element
+  if (tiny_fits(kl, ku)) return gbtrf_tiny_run<T>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
   // bands whose window fits the register file: one lane per window column
   if (reg_class<T>(kl, ku)) return gbtrf_reg_run<T>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
   const i64 bytes = gbtrf_smem_elems<kP>((int)kl, (int)ku) * (i64)sizeof(T);
@@ -587,6 +589,8 @@ static int gbtrs_impl(char trans, i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, 
   // the register-window sweeps (one warp per 32 right-hand sides) where the band fits
   if (notr && sizeof(T) == 4 && reg_solve_fits<T>(kl, ku))
     return gbtrs_reg_run<T>(n, kl, ku, nrhs, ab, ldab, ipiv, B, ldb, stream, name);
+  // tiny bands: a warp per right-hand side, a lane per window row
+  if (notr && tiny_solve_fits(kl, ku)) return gbtrs_tiny_run<T>(n, kl, ku, nrhs, ab, ldab, ipiv, B, ldb, stream, name);
   const int ch = gbtrs_chunk_for<T>((int)kl, (int)ku, 227 * 1024);
   if (ch == 0) {
     set_error("%s: band too wide for the staged solve", name);

@@ -621,6 +621,21 @@ namespace bm {
 template <typename T>
 int gbtrf_reg_run(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
                   const char* name);
+// Tiny bands (lureg.cu): kl >= 1 and kl * (kl + ku + 1) <= 32 for the factorization (one
+// warp, a lane per window element), kl + ku + 1 <= 32 for the 'N' solve (a warp per
+// right-hand side).
+__host__ __device__ inline bool tiny_fits(long long kl, long long ku) {
+  return kl >= 1 && ku >= 0 && kl * (kl + ku + 1) <= 32;
+}
+__host__ __device__ inline bool tiny_solve_fits(long long kl, long long ku) {
+  return kl >= 0 && ku >= 0 && kl + ku + 1 <= 32;
+}
+template <typename T>
+int gbtrf_tiny_run(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
+                   const char* name);
+template <typename T>
+int gbtrs_tiny_run(i64 n, i64 kl, i64 ku, i64 nrhs, const T* ab, i64 ldab, const i64* ipiv, T* B, i64 ldb,
+                   cudaStream_t stream, const char* name);
 // gbtrs 'N' by one warp per 32 right-hand sides; callers check reg_class<T>(kl, 0) and
 // reg_kv_class<T>(kl + ku) first.
 template <typename T>

@@ -39,7 +39,10 @@ def rel(a, b):
                                          # every register-window size class of kl and kl + ku
                                          (300, 40, 8, 0.0), (300, 49, 30, 0.0), (300, 20, 70, 0.0),
                                          (300, 12, 100, 0.0), (500, 56, 40, 5.0), (260, 6, 2, 0.0),
-                                         (260, 12, 3, 0.0), (260, 24, 8, 0.0)])
+                                         (260, 12, 3, 0.0), (260, 24, 8, 0.0),
+                                         # tiny bands (a lane per window element)
+                                         (500, 1, 30, 0.0), (500, 3, 4, 0.0), (300, 2, 13, 0.0),
+                                         (37, 4, 3, 0.0), (3, 2, 1, 0.0)])
 def test_gbtrf_gbtrs_bitexact(bm, gpu, orc, dt, n, l, u, shift):
     rng = np.random.default_rng(n * 131 + l * 7 + u)
     data = rng.standard_normal((l + u + 1, n)).astype(dt)
