@@ -111,7 +111,10 @@ __global__ void __launch_bounds__(32) gbtrf_tiny_kernel(i64 m, i64 n, int kl, in
   for (int s = 0; s < kTinyPre; ++s) e[s] = enter ? elem(s + 1 + kl, s + 1 + c) : T(0);
   const int src_next = min((c + 1) * kl + r, 31), src_row1 = min((c + 1) * kl, 31);
   i64 inf = 0;
-  for (i64 j = 0; j < mn; ++j) {
+  // one step on ring slot `ent`: its value enters at the slide, and the slot is then
+  // reloaded for step j + kTinyPre (a slot is only read at its own step, so no
+  // instruction waits on a load in flight)
+  auto step = [&](i64 j, T& ent) {
     const int km = (int)min((i64)kl, m - 1 - j);
     unsigned long long key = 0ull;
     int idx = 0x7fffffff;
@@ -153,11 +156,14 @@ __global__ void __launch_bounds__(32) gbtrf_tiny_kernel(i64 m, i64 n, int kl, in
     const T na = __shfl_sync(0xffffffffu, a, src_next);
     const T nu = __shfl_sync(0xffffffffu, a, src_row1);
     const bool inside = c + 1 <= kv;
-    a = r < kl ? (inside ? na : T(0)) : e[0];
+    a = r < kl ? (inside ? na : T(0)) : ent;
     u = inside ? nu : T(0);
+    ent = enter ? elem(j + kTinyPre + 1 + kl, j + kTinyPre + 1 + c) : T(0);
+  };
+  for (i64 j = 0; j < mn; j += kTinyPre) {
 #pragma unroll
-    for (int s = 0; s + 1 < kTinyPre; ++s) e[s] = e[s + 1];
-    e[kTinyPre - 1] = enter ? elem(j + kTinyPre + 1 + kl, j + kTinyPre + 1 + c) : T(0);
+    for (int s = 0; s < kTinyPre; ++s)
+      if (j + s < mn) step(j + s, e[s]);
   }
   // m < n: the fill rows of columns mn+ku+1 .. mn+kv-1 at rows >= mn (no step reaches them)
   for (i64 cc = mn + ku + 1 + lane; cc < min(mn + kv, n); cc += 32)
@@ -192,10 +198,10 @@ __global__ void __launch_bounds__(32) gbtrs_tiny_kernel(i64 n, int kl, int ku, i
     if (kl > 0 && n > 1) {
       const bool act = lane <= kl;
       T x = (act && lane < n) ? b[lane] : T(0);
+      // ring slot s holds, for its step j: lv = L(j+lane, j) (lanes 1..kl), pv = ipiv(j),
+      // ev = b(j+1+kl); a slot is read at its own step only, then reloaded kTinyPre ahead
       T lv[kTinyPre], ev[kTinyPre];
       i64 pv[kTinyPre];
-      // at step j: lv = L(j+lane, j) (lanes 1..kl), pv = ipiv(j), ev = b(j+1+kl); the loaded
-      // values are only moved until their step (arithmetic on them would wait for the load)
       auto fetch = [&](i64 j, T& l_, i64& p_, T& e_) {
         const bool ok = j < n - 1;
         l_ = (ok && lane >= 1 && lane <= kl && j + lane < n) ? ab[(kv + lane) + j * ldab] : T(0);
@@ -204,8 +210,8 @@ __global__ void __launch_bounds__(32) gbtrs_tiny_kernel(i64 n, int kl, int ku, i
       };
 #pragma unroll
       for (int s = 0; s < kTinyPre; ++s) fetch(s, lv[s], pv[s], ev[s]);
-      for (i64 j = 0; j < n - 1; ++j) {
-        const int jp = (int)(pv[0] - 1 - j);
+      auto step = [&](i64 j, T& l_, i64& p_, T& e_) {
+        const int jp = (int)(p_ - 1 - j);
         const int lm = (int)min((i64)kl, n - 1 - j);
         if (jp != 0) {
           const T t = __shfl_sync(0xffffffffu, x, jp);
@@ -213,55 +219,61 @@ __global__ void __launch_bounds__(32) gbtrs_tiny_kernel(i64 n, int kl, int ku, i
           if (lane == 0) x = t;
           if (lane == jp) x = x0;
         }
-        if (lane == 0 && j < n) b[j] = x;  // b(j) is final
+        if (lane == 0) b[j] = x;  // b(j) is final
         const T bj = __shfl_sync(0xffffffffu, x, 0);
-        if (is_nonzero(bj) && lane >= 1 && lane <= lm) x = fma(lv[0], -bj, x);
+        if (is_nonzero(bj) && lane >= 1 && lane <= lm) x = fma(l_, -bj, x);
         const T nx = __shfl_sync(0xffffffffu, x, min(lane + 1, 31));
-        x = lane < kl ? nx : ev[0];
+        x = lane < kl ? nx : e_;
+        fetch(j + kTinyPre, l_, p_, e_);
+      };
+      for (i64 j = 0; j < n - 1; j += kTinyPre) {
 #pragma unroll
-        for (int s = 0; s + 1 < kTinyPre; ++s) {
-          lv[s] = lv[s + 1];
-          pv[s] = pv[s + 1];
-          ev[s] = ev[s + 1];
-        }
-        fetch(j + kTinyPre, lv[kTinyPre - 1], pv[kTinyPre - 1], ev[kTinyPre - 1]);
+        for (int s = 0; s < kTinyPre; ++s)
+          if (j + s < n - 1) step(j + s, lv[s], pv[s], ev[s]);
       }
-      // the last rows of the window are final
-      if (act && n - 1 + lane < n) b[n - 1 + lane] = x;
+      // the last row of the window is final
+      if (lane == 0) b[n - 1] = x;
     }
     __syncwarp();
     {
       const bool act = lane <= kv;
       T x = (act && n - 1 - lane >= 0) ? b[n - 1 - lane] : T(0);
+      // ring slot s, for its step j: uv = U(j-lane, j) (lanes 0..kv; lane 0: U(j, j)),
+      // ev = b(j-1-kv)
       T uv[kTinyPre], ev[kTinyPre];
-      // at step j: uv = U(j-lane, j) (lanes 0..kv; lane 0: U(j, j)), ev = b(j-1-kv)
       auto fetch = [&](i64 j, T& u_, T& e_) {
         u_ = (j >= 0 && act && j - lane >= 0) ? ab[(kv - lane) + j * ldab] : T(0);
         e_ = (j >= 0 && lane == kv && j - 1 - kv >= 0) ? b[j - 1 - kv] : T(0);
       };
 #pragma unroll
       for (int s = 0; s < kTinyPre; ++s) fetch(n - 1 - s, uv[s], ev[s]);
-      T yh = T(0), yl = T(0);  // the reciprocal pair of U(j0 - lane, j0 - lane), refreshed every 32 steps
-      for (i64 j = n - 1; j >= 0; --j) {
+      // the reciprocal pairs of U's diagonal, 32 steps at a time (lane k: step j0 - k);
+      // the next block's diagonal is loaded a block ahead
+      T yh = T(0), yl = T(0);
+      T dnext = (n - 1 - lane >= 0) ? ab[kv + (n - 1 - lane) * ldab] : T(1);
+      auto step = [&](i64 j, T& u_, T& e_) {
         const int k = (int)((n - 1 - j) & 31);
-        if (k == 0 && j - lane >= 0) div_rcp(ab[kv + (j - lane) * ldab], yh, yl);
-        const T d = __shfl_sync(0xffffffffu, uv[0], 0);  // U(j, j)
+        if (k == 0) {
+          div_rcp(dnext, yh, yl);
+          dnext = (j - 32 - lane >= 0) ? ab[kv + (j - 32 - lane) * ldab] : T(1);
+        }
+        const T d = __shfl_sync(0xffffffffu, u_, 0);  // U(j, j)
         const T h = __shfl_sync(0xffffffffu, yh, k), lo = __shfl_sync(0xffffffffu, yl, k);
         T xj = __shfl_sync(0xffffffffu, x, 0);
         if (is_nonzero(xj)) {
           xj = div_staged(xj, d, h, lo);
           if (lane == 0) x = xj;
-          if (lane >= 1 && act && j - lane >= 0) x = fma(-xj, uv[0], x);
+          if (lane >= 1 && act && j - lane >= 0) x = fma(-xj, u_, x);
         }
         if (lane == 0) b[j] = x;  // x(j) is final
         const T nx = __shfl_sync(0xffffffffu, x, min(lane + 1, 31));
-        x = lane < kv ? nx : ev[0];
+        x = lane < kv ? nx : e_;
+        fetch(j - kTinyPre, u_, e_);
+      };
+      for (i64 j = n - 1; j >= 0; j -= kTinyPre) {
 #pragma unroll
-        for (int s = 0; s + 1 < kTinyPre; ++s) {
-          uv[s] = uv[s + 1];
-          ev[s] = ev[s + 1];
-        }
-        fetch(j - kTinyPre, uv[kTinyPre - 1], ev[kTinyPre - 1]);
+        for (int s = 0; s < kTinyPre; ++s)
+          if (j - s >= 0) step(j - s, uv[s], ev[s]);
       }
     }
     __syncwarp();

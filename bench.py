@@ -823,6 +823,13 @@ def run_case(args):
         A.data[lu] += 2.0 * lu + 1.0
         b = torch.randn(n, dtype=dt, device=dev, generator=g)
         fn = lambda: A.solve(b)
+    elif parts[0] == "config1":
+        # the CPU-runnable case: brandn(10000,10000,4,3) + 10 I, A\b
+        n = args.n or 10000
+        A = bm.brandn(torch.float64, n, n, 4, 3, device=dev, generator=g)
+        A.data[3] += 10.0
+        b = torch.randn(n, dtype=torch.float64, device=dev, generator=g)
+        fn = lambda: A.solve(b)
     elif parts[0] == "refined":
         # the single-system refined solve (randn + 16 I, b randn), as refined_single times it
         n = args.n or (1 << 20)
