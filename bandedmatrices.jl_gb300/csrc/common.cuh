@@ -118,6 +118,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_
   return false;
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start before the previous kernel in the stream ends.
+// grid_dep_wait() returns once every prerequisite grid has completed and its memory is
+// visible; grid_dep_launch() lets the next such kernel start.  Both are no-ops for a
+// kernel launched the ordinary way.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);

@@ -89,6 +89,8 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_kernel(i64 m, i64 n, int
   const int kv = kl + ku, R = kl + NB, RS = R | 1;
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
+  grid_dep_wait();  // the previous replay's columns
+  grid_dep_launch();
   T* P = reinterpret_cast<T*>(smem_raw);  // panel: column c (0..jb-1) x row r (matrix row j0 + r)
   unsigned long long* wk = reinterpret_cast<unsigned long long*>(P + (i64)RS * NB);  // NW warp keys
   int* wi = reinterpret_cast<int*>(wk + NW);                                          // NW warp indices
@@ -196,6 +198,8 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_reg_kernel(i64 m, i64 n,
   const int kv = kl + ku, R = kl + NB;
   const i64 mn = min(m, n);
   const int jb = (int)min((i64)NB, mn - j0);
+  grid_dep_wait();  // the previous replay's columns
+  grid_dep_launch();
   T v[RPT][NB];  // v[i][q]: row tid + NT*i of column c + q at step c
 #pragma unroll
   for (int i = 0; i < RPT; ++i)
@@ -311,6 +315,17 @@ __global__ void __launch_bounds__(kReplayNT) gbtrf_replay_kernel(i64 m, i64 n, i
   const int jb = (int)min((i64)NB, mn - j0);
   const i64 t = first + blockIdx.x;
   T* L = reinterpret_cast<T*>(smem_raw);
+  T v[RPT];
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + NT * i;
+    const i64 row = j0 + r, d = row - t;
+    v[i] = (r < R && row < m && d >= -kv && d <= kl) ? ab[(kv + d) + t * ldab] : T(0);
+  }
+  // the column is complete (the previous replay ended before the panel began); the
+  // panel's multipliers and pivots are waited for
+  grid_dep_launch();
+  grid_dep_wait();
   for (int k = 0; k < jb; ++k) {  // asynchronous element copies, one wait
     const i64 gk = j0 + k;
     const int km = (int)min((i64)kl, m - 1 - gk);
@@ -320,13 +335,6 @@ __global__ void __launch_bounds__(kReplayNT) gbtrf_replay_kernel(i64 m, i64 n, i
   if (tid < jb) {  // -1: zero pivot (no interchange, no update)
     const i64 gj = j0 + tid;
     st[tid] = is_nonzero(ab[kv + gj * ldab]) ? (int)(ipiv[gj] - 1 - gj) : -1;
-  }
-  T v[RPT];
-#pragma unroll
-  for (int i = 0; i < RPT; ++i) {
-    const int r = tid + NT * i;
-    const i64 row = j0 + r, d = row - t;
-    v[i] = (r < R && row < m && d >= -kv && d <= kl) ? ab[(kv + d) + t * ldab] : T(0);
   }
   cp_async_wait<0>();
   __syncthreads();
@@ -371,6 +379,25 @@ inline int replay_rpt(i64 kl) {
   return r <= 1 ? 1 : r <= 2 ? 2 : r <= 3 ? 3 : r <= 4 ? 4 : r <= 5 ? 5 : r <= 6 ? 6 : r <= 8 ? 8 : r <= 12 ? 12 : 16;
 }
 
+// Launch with programmatic stream serialization: the kernel may begin while the previous
+// one in the stream finishes, and waits for it with grid_dep_wait() before reading its
+// results.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                    cudaStream_t stream, Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <typename T>
 static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
                            const char* name) {
@@ -410,33 +437,41 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
   const i64 mn = std::min(m, n);
   for (i64 j0 = 0; j0 < mn; j0 += kNB) {
     const i64 jb = std::min<i64>(kNB, mn - j0);
+    cudaError_t le;
     switch (prpt) {
       case 1:
-        gbtrf_panel_reg_kernel<T, 1><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 1>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+                              ldab, ipiv, info);
         break;
       case 2:
-        gbtrf_panel_reg_kernel<T, 2><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 2>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+                              ldab, ipiv, info);
         break;
       case 3:
-        gbtrf_panel_reg_kernel<T, 3><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 3>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+                              ldab, ipiv, info);
         break;
       case 4:
         if constexpr (sizeof(T) == 4) {
-          gbtrf_panel_reg_kernel<T, 4><<<1, kPanelNT, 0, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+          le = launch_dependent(gbtrf_panel_reg_kernel<T, 4>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+                                ldab, ipiv, info);
           break;
         }
         [[fallthrough]];
       default:
-        gbtrf_panel_kernel<T><<<1, kPanelNT, (int)pbytes, stream>>>(m, n, (int)kl, (int)ku, j0, ab, ldab, ipiv, info);
+        le = launch_dependent(gbtrf_panel_kernel<T>, 1, kPanelNT, (size_t)pbytes, stream, m, n, (int)kl, (int)ku, j0,
+                              ab, ldab, ipiv, info);
     }
+    if ((r = cuda_status(le, name))) return r;
     if ((r = launch_status(name))) return r;
     const i64 first = j0 + jb, last = std::min(n, j0 + jb + kl + ku);
     if (last > first) {
-      with_replay([&](auto kern) {
-        kern<<<(unsigned)(last - first), kReplayNT, (int)rbytes, stream>>>(m, n, (int)kl, (int)ku, j0, first, ab, ldab,
-                                                                          ipiv);
-        return 0;
-      });
+      r = cuda_status(with_replay([&](auto kern) {
+                        return launch_dependent(kern, (unsigned)(last - first), kReplayNT, (size_t)rbytes, stream, m, n,
+                                                (int)kl, (int)ku, j0, first, ab, ldab, ipiv);
+                      }),
+                      name);
+      if (r) return r;
       if ((r = launch_status(name))) return r;
     }
   }
