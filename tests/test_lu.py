@@ -481,3 +481,29 @@ def test_solve_division_is_correctly_rounded(bm, gpu, orc, ku):
     bd = torch.from_numpy(b.copy()).to(gpu)
     assert np.array_equal(F.solve(bd).cpu().numpy().view(np.int64), want.view(np.int64))
     assert np.array_equal(F.T.solve(bd).cpu().numpy().view(np.int64), want.view(np.int64))
+
+
+@pytest.mark.parametrize("m,n,l,u", [(400, 400, 4, 3), (300, 260, 2, 1), (260, 300, 1, 30), (40, 33, 3, 4)])
+def test_tiny_bands_special_values(bm, gpu, orc, m, n, l, u):
+    """The tiny-band kernels (a lane per window element) on rectangular shapes, with zero
+    columns (info), NaN and infinity in the band: factors, pivots and info equal
+    dgbtf2's bit for bit (NaN where dgbtf2 has NaN), and square systems solve as dgbtrs."""
+    rng = np.random.default_rng(m * 7 + n + l * 3 + u)
+    data = rng.standard_normal((l + u + 1, n))
+    data[:, n // 3] = 0.0
+    data[u, n // 2] = np.nan
+    data[max(u - 1, 0), 2 * n // 3] = np.inf
+    data[u, 5] = 1e-310  # a subnormal pivot candidate
+    A = dev_band(bm, data, m, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(m, n, l, u, orc.lu_storage(data, n, l, u))
+    assert F.info == info
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+    got = F.factors.data.cpu().numpy()
+    mask = orc.band_to_dense(np.ones_like(LU), m, l, l + u) != 0
+    assert np.array_equal(orc.band_to_dense(got, m, l, l + u)[mask], orc.band_to_dense(LU, m, l, l + u)[mask],
+                          equal_nan=True)
+    if m == n:
+        b = rng.standard_normal((n, 2))
+        x = F.solve(torch.from_numpy(b).to(gpu)).cpu().numpy()
+        assert np.array_equal(x, orc.gbtrs("N", n, l, u, LU, ipiv, b), equal_nan=True)
