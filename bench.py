@@ -393,20 +393,13 @@ def run_gpu(args, rank, world):
         graphs.append((lab, gr, nb))
     ev = {lab: [] for lab, _, _ in graphs}
 
-    def step(record):
-        for lab, gr, nb in graphs:
-            if record:
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
+    def step():
+        for _, gr, _ in graphs:
             gr.replay()
-            if record:
-                e1.record(stream)
-                ev[lab].append((e0, e1))
 
     with ClockSampler(dev.index) as clk:
         for _ in range(args.warmup):
-            step(False)
+            step()
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
@@ -415,8 +408,22 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
         t0.record(stream)
         for _ in range(args.steps):
-            step(True)
+            step()
         t1.record(stream)
+        torch.cuda.synchronize()
+        # Per-case figures: each case's graph replayed back to back, the first replay
+        # untimed.  A kernel then inherits only its own write-backs of dirty L2 lines;
+        # inside the step it inherits the previous case's (up to ~100 MB after the
+        # Float64 product), which the sweep step total above includes.
+        for lab, gr, _ in graphs:
+            gr.replay()
+            for _ in range(args.steps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                gr.replay()
+                e1.record(stream)
+                ev[lab].append((e0, e1))
         torch.cuda.synchronize()
     ms = t0.elapsed_time(t1)
     if world > 1:
