@@ -41,16 +41,15 @@ __global__ void __launch_bounds__(32 * G) gbtrs_one_kernel(bool trans, i64 n, in
 // ------------------------------------------------------------------ wide bands
 // Bands whose one-column window does not fit one CTA's shared memory (e.g. kl = ku =
 // 128 or 512 in Float64): the factorization runs panel by panel over the gbtrf storage
-// in global memory, as two launches per panel of kNB columns.
-//   * gbtrf_panel_kernel (one CTA of 256 threads): loads the panel -- rows j0 ..
-//     j0+kl+kNB-1 of its kNB columns -- into shared memory and takes dgbtf2's steps on
-//     it: the pivot search (warp argmax, then across warps), the interchange within the
-//     panel's later columns, the reciprocal of the pivot (one thread), and the scaling
-//     and rank-1 update by one thread per row (rows beyond 256 wrap).  It stores the
-//     panel back (L in dgbtf2's format) with the pivots.
+// in global memory, as two launches per panel of NB columns (NB = 8 or 4, chosen by kl;
+// 16 for the shared-memory panel).
+//   * gbtrf_panel_reg_kernel (one CTA of 256 threads) holds the panel -- rows j0 ..
+//     j0+kl+NB-1 of its NB columns -- in registers and takes dgbtf2's steps on it (see
+//     below); gbtrf_panel_kernel does the same in shared memory for the widest bands.
+//     Either stores the panel back (L in dgbtf2's format) with the pivots.
 //   * gbtrf_replay_kernel (one CTA of kReplayNT threads per column, one warp per
 //     sub-partition): every column the panel's steps can reach (up to kl+ku to its
-//     right) replays the steps in order on its rows j0 .. j0+kl+kNB-1, held in
+//     right) replays the steps in order on its rows j0 .. j0+kl+NB-1, held in
 //     registers (row r by thread r mod kReplayNT).  At each step the threads holding the
 //     pivot row and row k publish both values through shared memory, one barrier, and
 //     every thread applies the interchange and its rows' fmas; the multipliers are
@@ -177,8 +176,8 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_kernel(i64 m, i64 n, int
   if (tid == 0) *info = inf;
 }
 
-// Register panel (R = kl + kNB <= RPT * kPanelNT rows): thread t holds rows t + kPanelNT*i
-// of the panel's columns in registers, the column of the current step at index 0 (the
+// Register panel of NB columns (R = kl + NB <= RPT * kPanelNT rows): thread t holds rows
+// t + kPanelNT*i of the panel's columns in registers, the column of the current step at index 0 (the
 // window rotates by one column per step, and the finished column is stored).  A step:
 // the key of each row, a warp argmax, the warps' results through shared memory (one
 // barrier); the threads holding the pivot row and row c publish both rows and the
@@ -187,10 +186,10 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_kernel(i64 m, i64 n, int
 // traffic for the elements themselves.  (Measured against two alternatives at
 // kl = 128: four warps with two rows per thread, 41 us per panel, and rows rotating
 // out of the active slots with a uniform zero mask, 45 us, against 33 us for this one.)
-template <typename T, int RPT>
+template <typename T, int RPT, int NB>
 __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_reg_kernel(i64 m, i64 n, int kl, int ku, i64 j0, T* ab,
                                                                     i64 ldab, i64* ipiv, i64* info) {
-  constexpr int NT = kPanelNT, NB = kNB, NW = NT / 32;
+  constexpr int NT = kPanelNT, NW = NT / 32;
   __shared__ unsigned long long wk[2][NW];
   __shared__ int wi[2][NW];
   __shared__ T prow[2][NB], crow[2][NB], srcp[2];
@@ -298,15 +297,15 @@ __global__ void __launch_bounds__(kPanelNT) gbtrf_panel_reg_kernel(i64 m, i64 n,
 // (RPT of them) in registers.  smem: the panel's multipliers, L[k*RS + r] for the row
 // j0 + r at step k.
 template <typename T>
-__host__ __device__ constexpr i64 replay_smem_bytes(int kl) {
-  return (i64)((kl + kNB) | 1) * kNB * (i64)sizeof(T);
+__host__ __device__ constexpr i64 replay_smem_bytes(int kl, int nb) {
+  return (i64)((kl + nb) | 1) * nb * (i64)sizeof(T);
 }
 
-template <typename T, int RPT>
+template <typename T, int RPT, int NB>
 __global__ void __launch_bounds__(kReplayNT) gbtrf_replay_kernel(i64 m, i64 n, int kl, int ku, i64 j0, i64 first,
                                                                   T* ab, i64 ldab, const i64* ipiv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NB = kNB, NT = kReplayNT;
+  constexpr int NT = kReplayNT;
   __shared__ int st[NB];
   __shared__ T xch[2][2];  // [step parity][0: the pivot row's value, 1: row k's value]
   const int tid = threadIdx.x;
@@ -373,9 +372,9 @@ __global__ void __launch_bounds__(kReplayNT) gbtrf_replay_kernel(i64 m, i64 n, i
   }
 }
 
-// rows held per replay thread: a class >= ceil((kl + kNB) / kReplayNT)
-inline int replay_rpt(i64 kl) {
-  const i64 r = ceil_div(kl + kNB, (i64)kReplayNT);
+// rows held per replay thread: a class >= ceil((kl + nb) / kReplayNT)
+inline int replay_rpt(i64 kl, int nb) {
+  const i64 r = ceil_div(kl + nb, (i64)kReplayNT);
   return r <= 1 ? 1 : r <= 2 ? 2 : r <= 3 ? 3 : r <= 4 ? 4 : r <= 5 ? 5 : r <= 6 ? 6 : r <= 8 ? 8 : r <= 12 ? 12 : 16;
 }
 
@@ -398,31 +397,35 @@ static cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, uns
   return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
-template <typename T>
-static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
-                           const char* name) {
-  const i64 pbytes = panel_smem_bytes<T>((int)kl), rbytes = replay_smem_bytes<T>((int)kl);
-  if (pbytes > 227 * 1024 || kl + kNB > 16 * kReplayNT) {
+template <typename T, int NB>
+static int gbtrf_wide_run(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
+                          const char* name) {
+  const i64 pbytes = panel_smem_bytes<T>((int)kl), rbytes = replay_smem_bytes<T>((int)kl, NB);
+  if (pbytes > 227 * 1024 || kl + NB > 16 * kReplayNT) {
     set_error("%s: band (kl=%lld) exceeds the panel limit", name, (long long)kl);
     return BM_ERR_UNSUPPORTED;
   }
-  const int rpt = replay_rpt(kl);
+  const int rpt = replay_rpt(kl, NB);
   // f(kernel) for the replay kernel of this band's row class
   auto with_replay = [&](auto&& f) {
     switch (rpt) {
 #define BM_RPT(v) \
   case v:         \
-    return f(gbtrf_replay_kernel<T, v>);
+    return f(gbtrf_replay_kernel<T, v, NB>);
       BM_RPT(1) BM_RPT(2) BM_RPT(3) BM_RPT(4) BM_RPT(5) BM_RPT(6) BM_RPT(8) BM_RPT(12)
 #undef BM_RPT
       default:
-        return f(gbtrf_replay_kernel<T, 16>);
+        return f(gbtrf_replay_kernel<T, 16, NB>);
     }
   };
   // the register panel where the panel's rows fit RPT rows per thread (at most 3 in
   // Float64, 4 in Float32, within the register file); else the shared-memory panel
-  const int prpt_need = (int)ceil_div(kl + kNB, (i64)kPanelNT);
+  const int prpt_need = (int)ceil_div(kl + NB, (i64)kPanelNT);
   const int prpt = prpt_need <= (sizeof(T) == 8 ? 3 : 4) ? prpt_need : 0;
+  if (!prpt && NB != kNB) {  // the shared-memory panel is kNB columns wide
+    set_error("%s: internal panel width %d without a register panel", name, NB);
+    return BM_ERR_UNSUPPORTED;
+  }
   int r = cuda_status(ensure_smem((const void*)gbtrf_panel_kernel<T>, (int)pbytes), name);
   if (r) return r;
   r = cuda_status(with_replay([&](auto kern) { return ensure_smem((const void*)kern, (int)rbytes); }), name);
@@ -435,25 +438,25 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
     if ((r = launch_status(name))) return r;
   }
   const i64 mn = std::min(m, n);
-  for (i64 j0 = 0; j0 < mn; j0 += kNB) {
-    const i64 jb = std::min<i64>(kNB, mn - j0);
+  for (i64 j0 = 0; j0 < mn; j0 += NB) {
+    const i64 jb = std::min<i64>(NB, mn - j0);
     cudaError_t le;
     switch (prpt) {
       case 1:
-        le = launch_dependent(gbtrf_panel_reg_kernel<T, 1>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 1, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
                               ldab, ipiv, info);
         break;
       case 2:
-        le = launch_dependent(gbtrf_panel_reg_kernel<T, 2>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 2, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
                               ldab, ipiv, info);
         break;
       case 3:
-        le = launch_dependent(gbtrf_panel_reg_kernel<T, 3>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+        le = launch_dependent(gbtrf_panel_reg_kernel<T, 3, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
                               ldab, ipiv, info);
         break;
       case 4:
         if constexpr (sizeof(T) == 4) {
-          le = launch_dependent(gbtrf_panel_reg_kernel<T, 4>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
+          le = launch_dependent(gbtrf_panel_reg_kernel<T, 4, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
                                 ldab, ipiv, info);
           break;
         }
@@ -476,6 +479,22 @@ static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* i
     }
   }
   return BM_OK;
+}
+
+// Panel width of the wide-band factorization: the panel's bulk update grows with the
+// width (about (NB-1)/2 columns x kl rows per step, on one SM), the launches per column
+// shrink with it.  Measured (Float64, GB300): kl = 128 -> 2.46 / 1.97 / 2.08 us per column
+// for NB = 16 / 8 / 4; kl = 512 -> 7.31 / 5.10 / 4.48.  Bands too wide for the register
+// panel take the 16-column shared-memory panel.
+template <typename T>
+static int gbtrf_wide_impl(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ipiv, i64* info, cudaStream_t stream,
+                           const char* name) {
+  const int maxr = sizeof(T) == 8 ? 3 : 4;
+  if (kl > 256 && ceil_div(kl + 4, (i64)kPanelNT) <= maxr)
+    return gbtrf_wide_run<T, 4>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
+  if (ceil_div(kl + 8, (i64)kPanelNT) <= maxr)
+    return gbtrf_wide_run<T, 8>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
+  return gbtrf_wide_run<T, kNB>(m, n, kl, ku, ab, ldab, ipiv, info, stream, name);
 }
 
 // Factor + solve of one system of a batch by a group of G warps.
