@@ -531,11 +531,11 @@ __device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i
 // whose band exceeds the bounds its part's shared memory was sized for (wkl/wku,
 // nkl/nku), gets info[s] = -(field number) and is skipped; an order entry outside
 // [0, count) is skipped.
-// The 4-warp variant is held to three CTAs per SM (at most 170 registers a thread):
-// with more registers the CTAs per SM drop to two, which costs a quarter of the
-// batch's throughput.
+// The Float64 4-warp variant is held to three CTAs per SM (at most 170 registers a
+// thread): with more registers the CTAs per SM drop to two, which costs a quarter of the
+// batch's throughput.  (Float32 would spill at that bound.)
 template <typename T, int W>
-__global__ void __launch_bounds__(32 * W, W == 4 ? 3 : 1) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
+__global__ void __launch_bounds__(32 * W, (W == 4 && sizeof(T) == 8) ? 3 : 1) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
                                                              const int32_t* __restrict__ order, i64 n_wide, T* AB,
                                                              i64* ipiv, T* B, i64* info, int32_t* counter,
                                                              i64 narrow_elems, i64 wkl, i64 wku, i64 nkl, i64 nku) {
