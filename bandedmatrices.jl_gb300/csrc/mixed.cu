@@ -183,6 +183,15 @@ __device__ __forceinline__ float abs_f32_of(double a) {
 }
 
 __device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
+// nan_max for non-negative a and b (absolute values): their IEEE bit patterns order as
+// the values do, with every NaN above infinity, so the maximum is an unsigned integer
+// comparison and stays off the FP64 pipe (two FP64 compares here would cost about as
+// much as two of the residual's fmas).
+__device__ __forceinline__ double nan_max_abs(double a, double b) {
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  return ub > ua ? b : a;
+}
 __device__ __forceinline__ float nan_maxf(float a, float b) { return (b > a || b != b) ? b : a; }
 
 // The tiles of one warp for right-hand sides [c0, c0+NR): residuals into R32 and the
@@ -258,9 +267,9 @@ __device__ void residual_tiles(const MixedParams& p, const bm_gb_desc& d, int c0
           const double b = Bs[i + c * ldb], x = Xs[i + c * ldb];
           const double r = b - y[c];
           Rs[i + (i64)c * n] = (float)r;
-          rn[c] = nan_max(rn[c], fabs(r));
-          xn[c] = nan_max(xn[c], fabs(x));
-          bn[c] = nan_max(bn[c], fabs(b));
+          rn[c] = nan_max_abs(rn[c], fabs(r));
+          xn[c] = nan_max_abs(xn[c], fabs(x));
+          bn[c] = nan_max_abs(bn[c], fabs(b));
         }
         an = nan_maxf(an, sabs);
       }
@@ -284,9 +293,9 @@ __device__ double residual_group(const MixedParams& p, const bm_gb_desc& d, int 
   for (int off = 16; off >= 1; off >>= 1) {
 #pragma unroll
     for (int c = 0; c < NR; ++c) {
-      rn[c] = nan_max(rn[c], __shfl_xor_sync(0xffffffffu, rn[c], off));
-      xn[c] = nan_max(xn[c], __shfl_xor_sync(0xffffffffu, xn[c], off));
-      bn[c] = nan_max(bn[c], __shfl_xor_sync(0xffffffffu, bn[c], off));
+      rn[c] = nan_max_abs(rn[c], __shfl_xor_sync(0xffffffffu, rn[c], off));
+      xn[c] = nan_max_abs(xn[c], __shfl_xor_sync(0xffffffffu, xn[c], off));
+      bn[c] = nan_max_abs(bn[c], __shfl_xor_sync(0xffffffffu, bn[c], off));
     }
     an = nan_maxf(an, __shfl_xor_sync(0xffffffffu, an, off));
   }
