@@ -832,10 +832,11 @@ __device__ void gbtrs_group(bool trans, i64 n, int kl, int ku, int nr, const T* 
                 for (int off = 16; off >= 1; off >>= 1) temp += __shfl_down_sync(0xffffffffu, temp, off);
                 if (lane == 0) smem[8 + wig] = temp;
                 Grp<G>::sync();
-                if (tid == 0) {
-                  T sum = smem[8];
-                  for (int w = 1; w < G; ++w) sum += smem[8 + w];
-                  X[s0 * nr + c] = fma(T(-1), sum, X[s0 * nr + c]);
+                if (wig == 0) {  // the warps' partials by a shuffle tree (log2 G dependent adds)
+                  T sum = lane < G ? smem[8 + lane] : T(0);
+#pragma unroll
+                  for (int off = G / 2; off >= 1; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+                  if (lane == 0) X[s0 * nr + c] = fma(T(-1), sum, X[s0 * nr + c]);
                 }
                 Grp<G>::sync();
               }
