@@ -507,3 +507,49 @@ def test_tiny_bands_special_values(bm, gpu, orc, m, n, l, u):
         b = rng.standard_normal((n, 2))
         x = F.solve(torch.from_numpy(b).to(gpu)).cpu().numpy()
         assert np.array_equal(x, orc.gbtrs("N", n, l, u, LU, ipiv, b), equal_nan=True)
+
+
+@pytest.mark.parametrize("dt,m,n,l,u", [(np.float64, 700, 700, 130, 140), (np.float64, 600, 640, 300, 40),
+                                        (np.float32, 520, 500, 260, 30)])
+def test_wide_band_special_values_and_graph_capture(bm, gpu, orc, dt, m, n, l, u):
+    """The wide-band panels (8 columns up to kl = 256, 4 above), launched with programmatic
+    stream serialization: NaN, infinity and zero columns give dgbtf2's factors, pivots and
+    info; the factorization captured in a CUDA graph and replayed gives the same bits."""
+    rng = np.random.default_rng(m + 3 * n + l + u)
+    data = rng.standard_normal((l + u + 1, n)).astype(dt)
+    data[:, n // 4] = 0.0
+    data[u, n // 2] = np.nan
+    data[u - 1, 3 * n // 4] = np.inf
+    A = dev_band(bm, data, m, l, u, gpu)
+    F = bm.lu(A)
+    LU, ipiv, info = orc.gbtf2(m, n, l, u, orc.lu_storage(data, n, l, u))
+    assert F.info == info
+    assert np.array_equal(F.ipiv.cpu().numpy(), ipiv)
+    mask = orc.band_to_dense(np.ones_like(LU), m, l, l + u) != 0
+    got = orc.band_to_dense(F.factors.data.cpu().numpy(), m, l, l + u)[mask]
+    assert np.array_equal(got, orc.band_to_dense(LU, m, l, l + u)[mask], equal_nan=True)
+    # the same factorization captured in a graph (a clean band, so that every step runs)
+    data2 = rng.standard_normal((l + u + 1, n)).astype(dt)
+    A2 = dev_band(bm, data2, m, l, u, gpu)
+    F2 = bm.lu(A2)  # first call outside capture (per-device set-up)
+    d = F2.factors.data
+    src = torch.zeros_like(d)
+    src[l:, :] = A2.data
+    info2 = torch.zeros(1, dtype=torch.int64, device=gpu)
+    s = torch.cuda.Stream(gpu)
+    s.wait_stream(torch.cuda.current_stream(gpu))
+    g = torch.cuda.CUDAGraph()
+    prefix = "d" if dt == np.float64 else "s"
+    with torch.cuda.graph(g, stream=s):
+        d.copy_(src)
+        bm._lib.call(f"bm_{prefix}gbtrf", m, n, l, u, d.data_ptr(), F2.factors.lda, F2.ipiv.data_ptr(),
+                     info2.data_ptr(), s.cuda_stream)
+    d.zero_()
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    LU2, ip2, inf2 = orc.gbtf2(m, n, l, u, orc.lu_storage(data2, n, l, u))
+    assert int(info2.item()) == inf2
+    assert np.array_equal(F2.ipiv.cpu().numpy(), ip2)
+    got2 = orc.band_to_dense(d.cpu().numpy(), m, l, l + u)[mask]
+    assert np.array_equal(got2, orc.band_to_dense(LU2, m, l, l + u)[mask])
