@@ -463,7 +463,7 @@ def _hard_quotients(rng, count):
     return b, d
 
 
-@pytest.mark.parametrize("ku", [0, 3, 200])
+@pytest.mark.parametrize("ku", [0, 3, 50, 200])  # tiny, tiny, narrow, wide sweeps
 def test_solve_division_is_correctly_rounded(bm, gpu, orc, ku):
     """The back substitution divides by U(j, j) through a staged reciprocal pair
     (Markstein's correction step) outside the ranges where it takes the plain division;
