@@ -456,8 +456,8 @@ static int gbtrf_wide_run(i64 m, i64 n, i64 kl, i64 ku, T* ab, i64 ldab, i64* ip
         break;
       case 4:
         if constexpr (sizeof(T) == 4) {
-          le = launch_dependent(gbtrf_panel_reg_kernel<T, 4, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0, ab,
-                                ldab, ipiv, info);
+          le = launch_dependent(gbtrf_panel_reg_kernel<T, 4, NB>, 1, kPanelNT, 0, stream, m, n, (int)kl, (int)ku, j0,
+                                ab, ldab, ipiv, info);
           break;
         }
         [[fallthrough]];
@@ -535,10 +535,10 @@ __device__ __forceinline__ void gbsv_system(const bm_gb_desc& d, int s, T* AB, i
 // thread): with more registers the CTAs per SM drop to two, which costs a quarter of the
 // batch's throughput.  (Float32 would spill at that bound.)
 template <typename T, int W>
-__global__ void __launch_bounds__(32 * W, (W == 4 && sizeof(T) == 8) ? 3 : 1) gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs,
-                                                             const int32_t* __restrict__ order, i64 n_wide, T* AB,
-                                                             i64* ipiv, T* B, i64* info, int32_t* counter,
-                                                             i64 narrow_elems, i64 wkl, i64 wku, i64 nkl, i64 nku) {
+__global__ void __launch_bounds__(32 * W, (W == 4 && sizeof(T) == 8) ? 3 : 1)
+    gbsv_batched_kernel(i64 count, const bm_gb_desc* __restrict__ descs, const int32_t* __restrict__ order,
+                        i64 n_wide, T* AB, i64* ipiv, T* B, i64* info, int32_t* counter, i64 narrow_elems, i64 wkl,
+                        i64 wku, i64 nkl, i64 nku) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* base = reinterpret_cast<T*>(smem_raw);
   int idx;
